@@ -1,0 +1,593 @@
+// C ABI entry points (include/hsdl.h): handles, validation, host<->device
+// copies and the calls into the generation / clean / query stages.
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hsdl_device.cuh"
+#include "hsdl_internal.h"
+#include "hsdl_runtime.h"
+
+namespace hsdl {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+std::atomic<int64_t>& launch_counter() {
+  static std::atomic<int64_t> c{0};
+  return c;
+}
+
+int device_sm_count() {
+  static int cached = 0;
+  if (cached == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      cached = v;
+    else
+      return 1;
+  }
+  return cached;
+}
+
+std::vector<int32_t> wave_schedule(int32_t n, int32_t first, int32_t max_wave);
+int32_t auto_max_wave(int32_t n, int64_t budget_bytes);
+
+}  // namespace hsdl
+
+using namespace hsdl;
+
+struct hsdl_host_graph {
+  HostGraph g;
+};
+
+#define HSDL_CHECK_ARG(cond, msg)   \
+  do {                              \
+    if (!(cond)) {                  \
+      set_error(msg);               \
+      return HSDL_ERR_INVALID;      \
+    }                               \
+  } while (0)
+
+namespace {
+
+int finish_host_graph(HostGraph&& g, hsdl_host_graph** out) {
+  auto* h = new hsdl_host_graph();
+  h->g = std::move(g);
+  *out = h;
+  return HSDL_OK;
+}
+
+int new_index(hsdl_index** out) {
+  auto* idx = new hsdl_index();
+  cudaError_t e = cudaStreamCreateWithFlags(&idx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete idx;
+    set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    return HSDL_ERR_CUDA;
+  }
+  *out = idx;
+  return HSDL_OK;
+}
+
+void free_index(hsdl_index* idx) {
+  if (!idx) return;
+  if (idx->stream) cudaStreamSynchronize(idx->stream);
+  idx->off.release();
+  idx->keys.release();
+  idx->par.release();
+  if (idx->stream) cudaStreamDestroy(idx->stream);
+  delete idx;
+}
+
+// Copies rows [v] of an index to the host (keys + parents).
+int fetch_row(hsdl_index* idx, int32_t v, std::vector<uint64_t>& k, std::vector<int32_t>& p) {
+  int64_t lo = idx->h_off[v], len = idx->h_off[v + 1] - lo;
+  k.resize(len);
+  p.resize(len);
+  if (len == 0) return HSDL_OK;
+  HSDL_CUDA(cudaMemcpy(k.data(), idx->keys.p + lo, len * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  HSDL_CUDA(cudaMemcpy(p.data(), idx->par.p + lo, len * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return HSDL_OK;
+}
+
+int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label* labels, hsdl_index* idx) {
+  HSDL_CHECK_ARG(n >= 1 && n <= (int32_t)kIdMask, "vertex count out of range");
+  HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
+  HSDL_CHECK_ARG(offsets && offsets[0] == 0, "offsets[0] must be 0");
+  int64_t total = offsets[n];
+  std::vector<uint64_t> keys((size_t)total);
+  std::vector<int32_t> par((size_t)total);
+  int64_t mr = 0;
+  for (int32_t v = 0; v < n; v++) {
+    HSDL_CHECK_ARG(offsets[v + 1] >= offsets[v], "offsets must be non-decreasing");
+    mr = std::max(mr, offsets[v + 1] - offsets[v]);
+    for (int64_t i = offsets[v]; i < offsets[v + 1]; i++) {
+      const hsdl_label& x = labels[i];
+      HSDL_CHECK_ARG(x.hub_vertex >= 0 && x.hub_vertex < n && x.hop >= 0 && x.hop <= K && x.distance >= 0,
+                     "label field out of range at entry " + std::to_string(i));
+      keys[i] = lkey((uint32_t)x.hub_vertex, (uint32_t)x.hop, (uint32_t)x.distance);
+      par[i] = x.parent_vertex;
+      HSDL_CHECK_ARG(i == offsets[v] || keys[i - 1] < keys[i],
+                     "row " + std::to_string(v) + " is not sorted by (hub, hop, distance)");
+    }
+  }
+  idx->n = n;
+  idx->K = K;
+  idx->total = total;
+  idx->before = idx->after = total;
+  idx->max_row = mr;
+  HSDL_TRY(idx->off.alloc((int64_t)n + 1));
+  HSDL_TRY(idx->keys.alloc(std::max<int64_t>(1, total)));
+  HSDL_TRY(idx->par.alloc(std::max<int64_t>(1, total)));
+  HSDL_CUDA(cudaMemcpy(idx->off.p, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice));
+  if (total > 0) {
+    HSDL_CUDA(cudaMemcpy(idx->keys.p, keys.data(), sizeof(uint64_t) * total, cudaMemcpyHostToDevice));
+    HSDL_CUDA(cudaMemcpy(idx->par.p, par.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice));
+  }
+  idx->h_off.assign(offsets, offsets + n + 1);
+  return HSDL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hsdl_last_error(void) { return last_error_cstr(); }
+int32_t hsdl_version(void) { return 1; }
+int64_t hsdl_launch_count(void) { return launch_counter().load(); }
+
+// ---------------------------------------------------------------------------
+// host graphs
+// ---------------------------------------------------------------------------
+int hsdl_gen_erdos_renyi(int32_t n, int64_t m, int32_t wmin, int32_t wmax, uint64_t seed, hsdl_host_graph** out) {
+  HSDL_CHECK_ARG(out && n >= 2 && n <= (int32_t)kIdMask, "n must be in [2, 2^28)");
+  HSDL_CHECK_ARG(m >= 0 && m <= (int64_t)n * (n - 1) / 2, "m out of range");
+  HSDL_CHECK_ARG(wmin >= 1 && wmax >= wmin, "weights must satisfy 1 <= wmin <= wmax");
+  HostGraph g;
+  gen_erdos_renyi(n, m, wmin, wmax, seed, g);
+  return finish_host_graph(std::move(g), out);
+}
+
+int hsdl_gen_chung_lu(int32_t n, double avg_degree, double exponent, double max_degree, int32_t wmin, int32_t wmax,
+                      uint64_t seed, hsdl_host_graph** out) {
+  HSDL_CHECK_ARG(out && n >= 2 && n <= (int32_t)kIdMask, "n must be in [2, 2^28)");
+  HSDL_CHECK_ARG(avg_degree > 0 && avg_degree < n - 1, "avg_degree out of range");
+  HSDL_CHECK_ARG(exponent > 1.0 && max_degree >= 1.0, "exponent must be > 1 and max_degree >= 1");
+  HSDL_CHECK_ARG(wmin >= 1 && wmax >= wmin, "weights must satisfy 1 <= wmin <= wmax");
+  HostGraph g;
+  gen_chung_lu(n, avg_degree, exponent, max_degree, wmin, wmax, seed, g);
+  return finish_host_graph(std::move(g), out);
+}
+
+int hsdl_gen_barabasi_albert(int32_t n, int32_t m0, int32_t wmin, int32_t wmax, uint64_t seed,
+                             hsdl_host_graph** out) {
+  HSDL_CHECK_ARG(out && n >= 2 && n <= (int32_t)kIdMask, "n must be in [2, 2^28)");
+  HSDL_CHECK_ARG(m0 >= 1 && m0 < n, "m0 must be in [1, n)");
+  HSDL_CHECK_ARG(wmin >= 1 && wmax >= wmin, "weights must satisfy 1 <= wmin <= wmax");
+  HostGraph g;
+  gen_barabasi_albert(n, m0, wmin, wmax, seed, g);
+  return finish_host_graph(std::move(g), out);
+}
+
+int hsdl_host_graph_from_edges(int32_t n, int64_t m, const int32_t* a, const int32_t* b, const int32_t* w,
+                               int32_t rank_by_degree, hsdl_host_graph** out) {
+  HSDL_CHECK_ARG(out && n >= 1 && n <= (int32_t)kIdMask, "n must be in [1, 2^28)");
+  HSDL_CHECK_ARG(m >= 0 && (m == 0 || (a && b && w)), "edge arrays missing");
+  // drop self loops and duplicate edges (the reference's add_edge keeps the
+  // last weight of a repeated edge, graph_v_of_v.h:90-108)
+  std::vector<std::pair<uint64_t, int64_t>> order;
+  order.reserve((size_t)m);
+  for (int64_t i = 0; i < m; i++) {
+    HSDL_CHECK_ARG(a[i] >= 0 && a[i] < n && b[i] >= 0 && b[i] < n, "edge endpoint out of range");
+    HSDL_CHECK_ARG(w[i] >= 1, "edge weights must be >= 1");
+    if (a[i] == b[i]) continue;
+    uint32_t x = (uint32_t)std::min(a[i], b[i]), y = (uint32_t)std::max(a[i], b[i]);
+    order.push_back({((uint64_t)x << 32) | y, i});
+  }
+  std::stable_sort(order.begin(), order.end(), [](const auto& p, const auto& q) { return p.first < q.first; });
+  std::vector<int32_t> ea, eb, ew;
+  for (size_t i = 0; i < order.size(); i++) {
+    if (i + 1 < order.size() && order[i + 1].first == order[i].first) continue;  // keep the last
+    ea.push_back((int32_t)(order[i].first >> 32));
+    eb.push_back((int32_t)(order[i].first & 0xffffffffu));
+    ew.push_back(w[order[i].second]);
+  }
+  HostGraph g;
+  build_ranked_csr(n, ea.data(), eb.data(), ew.data(), (int64_t)ea.size(), rank_by_degree != 0, g);
+  return finish_host_graph(std::move(g), out);
+}
+
+int hsdl_read_graph_text(const char* path, int32_t rank_by_degree, hsdl_host_graph** out) {
+  HSDL_CHECK_ARG(path && out, "null argument");
+  std::ifstream f(path);
+  if (!f) {
+    set_error(std::string("cannot open ") + path);
+    return HSDL_ERR_IO;
+  }
+  int64_t n = -1;
+  std::vector<int32_t> a, b, w;
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream ss(line);
+    std::string tag;
+    if (!(ss >> tag)) continue;
+    if (tag == "|V|=") {
+      ss >> n;
+    } else if (tag == "Edge") {
+      long long x, y;
+      double wt;
+      if (!(ss >> x >> y >> wt)) {
+        set_error("malformed Edge line: " + line);
+        return HSDL_ERR_IO;
+      }
+      a.push_back((int32_t)x);
+      b.push_back((int32_t)y);
+      w.push_back((int32_t)wt);  // the reference parses with stod into weight_type
+    }
+  }
+  HSDL_CHECK_ARG(n >= 1, "missing |V|= line");
+  return hsdl_host_graph_from_edges((int32_t)n, (int64_t)a.size(), a.data(), b.data(), w.data(), rank_by_degree, out);
+}
+
+int hsdl_host_graph_get(const hsdl_host_graph* g, int32_t* n, int64_t* adj_entries, const int64_t** row_ptr,
+                        const int32_t** col, const int32_t** w, const int32_t** new_to_old) {
+  HSDL_CHECK_ARG(g, "null graph");
+  if (n) *n = g->g.n;
+  if (adj_entries) *adj_entries = (int64_t)g->g.col.size();
+  if (row_ptr) *row_ptr = g->g.row_ptr.data();
+  if (col) *col = g->g.col.data();
+  if (w) *w = g->g.w.data();
+  if (new_to_old) *new_to_old = g->g.new_to_old.data();
+  return HSDL_OK;
+}
+
+void hsdl_host_graph_free(hsdl_host_graph* g) { delete g; }
+
+int hsdl_validate_csr(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w) {
+  HSDL_CHECK_ARG(n >= 1 && n <= (int32_t)kIdMask, "vertex count must be in [1, 2^28)");
+  HSDL_CHECK_ARG(row_ptr && (row_ptr[n] == 0 || (col && w)), "null CSR array");
+  std::string err = validate_csr(n, row_ptr, col, w);
+  if (!err.empty()) {
+    set_error(err);
+    return HSDL_ERR_INVALID;
+  }
+  return HSDL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device graphs
+// ---------------------------------------------------------------------------
+int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w, hsdl_graph** out) {
+  HSDL_CHECK_ARG(out, "null output");
+  HSDL_TRY(hsdl_validate_csr(n, row_ptr, col, w));
+  auto* g = new hsdl_graph();
+  g->n = n;
+  g->m2 = row_ptr[n];
+  g->h_rp.assign(row_ptr, row_ptr + n + 1);
+  std::vector<int2> adj((size_t)g->m2);
+  int32_t mw = 0;
+  for (int64_t e = 0; e < g->m2; e++) {
+    adj[e] = make_int2(col[e], w[e]);
+    mw = std::max(mw, w[e]);
+  }
+  g->max_w = mw;
+  int rc = g->rp.alloc((int64_t)n + 1);
+  if (rc == HSDL_OK) rc = g->adj.alloc(std::max<int64_t>(1, g->m2));
+  if (rc == HSDL_OK) {
+    cudaError_t e1 = cudaMemcpy(g->rp.p, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice);
+    cudaError_t e2 = g->m2 ? cudaMemcpy(g->adj.p, adj.data(), sizeof(int2) * g->m2, cudaMemcpyHostToDevice)
+                           : cudaSuccess;
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      set_error(std::string("graph upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+      rc = HSDL_ERR_CUDA;
+    }
+  }
+  if (rc != HSDL_OK) {
+    g->rp.release();
+    g->adj.release();
+    delete g;
+    return rc;
+  }
+  *out = g;
+  return HSDL_OK;
+}
+
+int hsdl_graph_destroy(hsdl_graph* g) {
+  if (!g) return HSDL_OK;
+  g->rp.release();
+  g->adj.release();
+  delete g;
+  return HSDL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// build / clean
+// ---------------------------------------------------------------------------
+void hsdl_build_opts_default(hsdl_build_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->struct_size = (int32_t)sizeof(hsdl_build_opts);
+  o->clean = 1;
+  o->first_wave = 1;
+}
+
+static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
+  hsdl_build_opts_default(o);
+  if (in) {
+    HSDL_CHECK_ARG(in->struct_size == (int32_t)sizeof(hsdl_build_opts), "hsdl_build_opts.struct_size mismatch");
+    *o = *in;
+  }
+  HSDL_CHECK_ARG(o->first_wave >= 0 && o->max_wave >= 0, "wave widths must be >= 0");
+  HSDL_CHECK_ARG(o->device_budget_bytes >= 0, "device_budget_bytes must be >= 0");
+  return HSDL_OK;
+}
+
+int hsdl_wave_bounds(int32_t n, const hsdl_build_opts* opts, int32_t* bounds, int32_t cap, int32_t* count) {
+  HSDL_CHECK_ARG(n >= 1 && count, "bad arguments");
+  hsdl_build_opts o;
+  HSDL_TRY(resolve_opts(opts, &o));
+  int64_t budget = o.device_budget_bytes;
+  if (budget == 0) {
+    size_t fb = 0, tb = 0;
+    if (cudaMemGetInfo(&fb, &tb) == cudaSuccess) budget = (int64_t)fb;
+  }
+  int32_t mw = o.max_wave > 0 ? o.max_wave : auto_max_wave(n, budget);
+  std::vector<int32_t> b = wave_schedule(n, o.first_wave > 0 ? o.first_wave : 1, mw);
+  *count = (int32_t)b.size();
+  if (bounds) {
+    HSDL_CHECK_ARG(cap >= (int32_t)b.size(), "bounds buffer too small");
+    std::copy(b.begin(), b.end(), bounds);
+  }
+  return HSDL_OK;
+}
+
+int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index** out) {
+  HSDL_CHECK_ARG(g && out, "null argument");
+  HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
+  HSDL_CHECK_ARG((int64_t)K * g->max_w < (int64_t)INT32_MAX, "K * max edge weight must be < 2^31");
+  hsdl_build_opts o;
+  HSDL_TRY(resolve_opts(opts, &o));
+  hsdl_index* idx = nullptr;
+  HSDL_TRY(new_index(&idx));
+  int rc = build_index(g, K, o, idx);
+  if (rc == HSDL_OK && o.clean) rc = clean_index(idx);
+  if (rc != HSDL_OK) {
+    free_index(idx);
+    return rc;
+  }
+  *out = idx;
+  return HSDL_OK;
+}
+
+int hsdl_clean(hsdl_index* idx) {
+  HSDL_CHECK_ARG(idx, "null index");
+  if (idx->cleaned) return HSDL_OK;
+  return clean_index(idx);
+}
+
+// ---------------------------------------------------------------------------
+// queries
+// ---------------------------------------------------------------------------
+int hsdl_query_batch_device(hsdl_index* idx, int64_t nq, const int32_t* d_s, const int32_t* d_t, const int32_t* d_k,
+                            int32_t* d_out, void* stream) {
+  HSDL_CHECK_ARG(idx && nq >= 0, "bad arguments");
+  if (nq == 0) return HSDL_OK;
+  HSDL_CHECK_ARG(d_s && d_t && d_k && d_out, "null query array");
+  cudaStream_t st = stream ? (cudaStream_t)stream : idx->stream;
+  return query_device(idx, nq, d_s, d_t, d_k, d_out, st);
+}
+
+int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
+                     int32_t* out) {
+  HSDL_CHECK_ARG(idx && nq >= 0, "bad arguments");
+  if (nq == 0) return HSDL_OK;
+  HSDL_CHECK_ARG(s && t && k && out, "null query array");
+  for (int64_t i = 0; i < nq; i++)
+    HSDL_CHECK_ARG(s[i] >= 0 && s[i] < idx->n && t[i] >= 0 && t[i] < idx->n,
+                   "query vertex out of range at query " + std::to_string(i));
+  cudaStream_t st = idx->stream;
+  int32_t* d = nullptr;
+  HSDL_CUDA(cudaMallocAsync(&d, sizeof(int32_t) * 4 * nq, st));
+  HSDL_CUDA(cudaMemcpyAsync(d, s, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
+  HSDL_CUDA(cudaMemcpyAsync(d + nq, t, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
+  HSDL_CUDA(cudaMemcpyAsync(d + 2 * nq, k, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
+  int rc = query_device(idx, nq, d, d + nq, d + 2 * nq, d + 3 * nq, st);
+  if (rc == HSDL_OK) {
+    HSDL_CUDA(cudaMemcpyAsync(out, d + 3 * nq, sizeof(int32_t) * nq, cudaMemcpyDeviceToHost, st));
+  }
+  HSDL_CUDA(cudaFreeAsync(d, st));
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  return rc;
+}
+
+// hop_constrained_extract_shortest_path (two_hop_labels.h:224-319): repeated
+// merge-joins that step from s and t to the parents of the best label pair.
+int hsdl_extract_path(hsdl_index* idx, int32_t s, int32_t t, int32_t k, int32_t* edges, int32_t cap,
+                      int32_t* n_edges) {
+  HSDL_CHECK_ARG(idx && n_edges && (cap == 0 || edges), "bad arguments");
+  HSDL_CHECK_ARG(s >= 0 && s < idx->n && t >= 0 && t < idx->n, "vertex out of range");
+  HSDL_CUDA(cudaStreamSynchronize(idx->stream));
+  int32_t cnt = 0;
+  std::vector<uint64_t> ks, kt;
+  std::vector<int32_t> ps, pt;
+  while (s != t) {
+    HSDL_TRY(fetch_row(idx, s, ks, ps));
+    HSDL_TRY(fetch_row(idx, t, kt, pt));
+    long long best = INT_MAX;
+    int32_t bs = -1, bt = -1;
+    size_t i = 0, j = 0;
+    while (i < ks.size() && j < kt.size()) {
+      uint32_t hi = lkey_hub(ks[i]), hj = lkey_hub(kt[j]);
+      if (hi == hj) {
+        size_t ie = i, je = j;
+        while (ie < ks.size() && lkey_hub(ks[ie]) == hi) ie++;
+        while (je < kt.size() && lkey_hub(kt[je]) == hj) je++;
+        for (size_t a = i; a < ie; a++) {
+          for (size_t b = j; b < je; b++) {
+            if ((int)(lkey_hop(kt[b]) + lkey_hop(ks[a])) <= k) {
+              long long d = (long long)lkey_dist(ks[a]) + lkey_dist(kt[b]);
+              if (best > d) {
+                best = d;
+                bs = ps[a];
+                bt = pt[b];
+              }
+            } else {
+              break;
+            }
+          }
+        }
+        i = ie;
+        j = je;
+      } else if (hi > hj) {
+        j++;
+      } else {
+        i++;
+      }
+    }
+    if (best >= INT_MAX) break;
+    if (s != bs) {
+      HSDL_CHECK_ARG(cnt < cap, "edge buffer too small");
+      edges[2 * cnt] = s;
+      edges[2 * cnt + 1] = bs;
+      cnt++;
+      s = bs;
+      k--;
+    }
+    if (t != bt) {
+      HSDL_CHECK_ARG(cnt < cap, "edge buffer too small");
+      edges[2 * cnt] = t;
+      edges[2 * cnt + 1] = bt;
+      cnt++;
+      t = bt;
+      k--;
+    }
+  }
+  *n_edges = cnt;
+  return HSDL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// index contents
+// ---------------------------------------------------------------------------
+int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
+  HSDL_CHECK_ARG(idx && info, "null argument");
+  info->n = idx->n;
+  info->K = idx->K;
+  info->cleaned = idx->cleaned ? 1 : 0;
+  info->waves = idx->waves;
+  info->labels = idx->total;
+  info->labels_before_clean = idx->before;
+  info->labels_after_clean = idx->after;
+  info->device_bytes = idx->off.bytes() + idx->keys.bytes() + idx->par.bytes();
+  info->time_generate_s = idx->t_gen;
+  info->time_sort_s = idx->t_sort;
+  info->time_clean_s = idx->t_clean;
+  info->max_row = idx->max_row;
+  return HSDL_OK;
+}
+
+int hsdl_export(hsdl_index* idx, int64_t* offsets, hsdl_label* labels) {
+  HSDL_CHECK_ARG(idx && offsets && (idx->total == 0 || labels), "null argument");
+  HSDL_CUDA(cudaStreamSynchronize(idx->stream));
+  std::vector<uint64_t> keys((size_t)idx->total);
+  std::vector<int32_t> par((size_t)idx->total);
+  if (idx->total > 0) {
+    HSDL_CUDA(cudaMemcpy(keys.data(), idx->keys.p, sizeof(uint64_t) * idx->total, cudaMemcpyDeviceToHost));
+    HSDL_CUDA(cudaMemcpy(par.data(), idx->par.p, sizeof(int32_t) * idx->total, cudaMemcpyDeviceToHost));
+  }
+  std::copy(idx->h_off.begin(), idx->h_off.end(), offsets);
+  for (int64_t i = 0; i < idx->total; i++) {
+    labels[i].hub_vertex = (int32_t)lkey_hub(keys[i]);
+    labels[i].parent_vertex = par[i];
+    labels[i].hop = (int32_t)lkey_hop(keys[i]);
+    labels[i].distance = (int32_t)lkey_dist(keys[i]);
+  }
+  return HSDL_OK;
+}
+
+int hsdl_import(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label* labels, hsdl_index** out) {
+  HSDL_CHECK_ARG(out && offsets, "null argument");
+  hsdl_index* idx = nullptr;
+  HSDL_TRY(new_index(&idx));
+  int rc = upload_index(n, K, offsets, labels, idx);
+  if (rc != HSDL_OK) {
+    free_index(idx);
+    return rc;
+  }
+  *out = idx;
+  return HSDL_OK;
+}
+
+// Clean_pc/main.cu:11-34 (save_labels): size_t V, then per vertex size_t n and
+// n records of 4 int32 (hub, parent, hop, distance).
+int hsdl_save_labels(hsdl_index* idx, const char* path) {
+  HSDL_CHECK_ARG(idx && path, "null argument");
+  std::vector<int64_t> off((size_t)idx->n + 1);
+  std::vector<hsdl_label> lab((size_t)std::max<int64_t>(1, idx->total));
+  HSDL_TRY(hsdl_export(idx, off.data(), lab.data()));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    set_error(std::string("cannot write ") + path);
+    return HSDL_ERR_IO;
+  }
+  size_t V = (size_t)idx->n;
+  bool ok = std::fwrite(&V, sizeof(size_t), 1, f) == 1;
+  for (int32_t v = 0; ok && v < idx->n; v++) {
+    size_t c = (size_t)(off[v + 1] - off[v]);
+    ok = std::fwrite(&c, sizeof(size_t), 1, f) == 1;
+    if (ok && c) ok = std::fwrite(lab.data() + off[v], sizeof(hsdl_label), c, f) == c;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) {
+    set_error(std::string("write failed: ") + path);
+    return HSDL_ERR_IO;
+  }
+  return HSDL_OK;
+}
+
+// Clean_pc/main.cu:36-58 (load_labels).
+int hsdl_load_labels(const char* path, int32_t K, hsdl_index** out) {
+  HSDL_CHECK_ARG(path && out, "null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    set_error(std::string("cannot open ") + path);
+    return HSDL_ERR_IO;
+  }
+  size_t V = 0;
+  bool ok = std::fread(&V, sizeof(size_t), 1, f) == 1 && V >= 1 && V <= kIdMask;
+  std::vector<int64_t> off(ok ? V + 1 : 1, 0);
+  std::vector<hsdl_label> lab;
+  for (size_t v = 0; ok && v < V; v++) {
+    size_t c = 0;
+    ok = std::fread(&c, sizeof(size_t), 1, f) == 1 && c <= ((size_t)1 << 40);
+    if (!ok) break;
+    size_t at = lab.size();
+    lab.resize(at + c);
+    if (c) ok = std::fread(lab.data() + at, sizeof(hsdl_label), c, f) == c;
+    off[v + 1] = (int64_t)lab.size();
+  }
+  std::fclose(f);
+  if (!ok) {
+    set_error(std::string("malformed label file: ") + path);
+    return HSDL_ERR_IO;
+  }
+  return hsdl_import((int32_t)V, K, off.data(), lab.empty() ? nullptr : lab.data(), out);
+}
+
+int hsdl_index_destroy(hsdl_index* idx) {
+  free_index(idx);
+  return HSDL_OK;
+}
+
+}  // extern "C"

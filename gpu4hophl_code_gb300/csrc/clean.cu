@@ -1,0 +1,244 @@
+// Canonical repair (clean) of a generated label set.
+//
+// Reference rule: hop_constrained_clean_L
+// (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:422-511).
+// For every vertex v, label (u, h, d) in L[v] is dropped iff some label
+// (w, h1, d1) of L[u] and some label (w, h2, d2) of v already accepted satisfy
+// h1 + h2 <= h and d1 + d2 <= d (:451-482).
+//
+// Parallel form.  The reference walks L[v] in order and checks against the
+// labels of v accepted so far.  For a label set that is a superset of the
+// canonical labels and whose every label is a real walk (what generation
+// produces), checking against *all* labels of v gives the same verdict: a
+// covering pair through a non-accepted label is itself a walk from u to v
+// through a hub ranked at or above u within h hops and distance d, so the
+// label is not canonical either way.  The one pair to exclude is the label
+// against itself: the only label of L[u] with hub u is u's self label
+// (u, 0, 0), so for hub w = u the check uses v's labels of hub u with fewer
+// than h hops.  Every label is therefore decided independently.
+//
+// Kernel: one block per vertex v (persistent blocks take vertices from a work
+// counter).  The block builds v's hop-prefix-min table T_v (hash on hub id, in
+// shared memory, or in a per-block global scratch area for very long rows),
+// then each warp takes labels (u, h, d) of v and scans L[u] with its lanes,
+// probing T_v and reducing with a warp-wide min.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+
+#include "hsdl_device.cuh"
+#include "hsdl_runtime.h"
+
+namespace hsdl {
+
+namespace {
+
+constexpr int kCleanThreads = 256;
+
+__device__ inline const int32_t* tab_find(const int32_t* T, uint32_t mask, int stride, int32_t w) {
+  uint32_t ix = table_hash((uint32_t)w, mask);
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    int32_t kk = T[(int64_t)ix * stride];
+    if (kk == w) return T + (int64_t)ix * stride;
+    if (kk == kEmptyKey) return nullptr;
+    ix = (ix + 1) & mask;
+  }
+  return nullptr;
+}
+
+__global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, const int64_t* __restrict__ off,
+                                                         const uint64_t* __restrict__ keys,
+                                                         uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
+                                                         int stride, int smem_slots, int32_t* __restrict__ gscratch,
+                                                         int64_t gscratch_slots, int* __restrict__ next_v) {
+  extern __shared__ int32_t smem_tab[];
+  __shared__ int s_v;
+  __shared__ int s_kept[kCleanThreads / 32];
+  const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_v = atomicAdd(next_v, 1);
+    __syncthreads();
+    const int v = s_v;
+    if (v >= n) break;
+    const int64_t lo = off[v];
+    const int len = (int)(off[v + 1] - lo);
+    int64_t cap = 8;
+    while (cap < 2 * (int64_t)len) cap <<= 1;
+    int32_t* T = (cap <= smem_slots) ? smem_tab : gscratch + (int64_t)blockIdx.x * gscratch_slots * stride;
+    const uint32_t mask = (uint32_t)cap - 1;
+    for (int64_t i = threadIdx.x; i < cap * stride; i += blockDim.x) T[i] = kInf32;
+    __syncthreads();
+    for (int j = threadIdx.x; j < len; j += blockDim.x) {
+      uint64_t k = keys[lo + j];
+      int32_t w = (int32_t)lkey_hub(k);
+      uint32_t ix = table_hash((uint32_t)w, mask);
+      bool placed = false;
+      for (uint32_t probe = 0; probe <= mask; probe++) {  // the table is at most half full
+        int32_t old = atomicCAS(&T[(int64_t)ix * stride], kEmptyKey, w);
+        if (old == kEmptyKey || old == w) {
+          placed = true;
+          break;
+        }
+        ix = (ix + 1) & mask;
+      }
+      if (placed) atomicMin(&T[(int64_t)ix * stride + 1 + lkey_hop(k)], (int32_t)lkey_dist(k));
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < cap; e += blockDim.x) {
+      int32_t* row = T + e * stride;
+      if (row[0] == kEmptyKey) continue;
+      int32_t m = row[1];
+      for (int j = 1; j <= K; j++) {
+        m = min(m, row[1 + j]);
+        row[1 + j] = m;
+      }
+    }
+    __syncthreads();
+    int my_kept = 0;
+    for (int i = wid; i < len; i += nw) {
+      uint64_t k = keys[lo + i];
+      int u = (int)lkey_hub(k);
+      int h = (int)lkey_hop(k);
+      long long d = (long long)lkey_dist(k);
+      bool keepit;
+      if (u == v) {
+        keepit = true;  // the self label (v, 0, 0) is never covered
+      } else {
+        long long q = LLONG_MAX;
+        // hub u itself: labels of v with hub u and fewer hops
+        const int32_t* ru = tab_find(T, mask, stride, u);
+        if (ru && ru[1 + h - 1] != kInf32) q = ru[1 + h - 1];
+        if (!(q <= d)) {
+          const int64_t ulo = off[u];
+          const int ulen = (int)(off[u + 1] - ulo);
+          for (int j0 = 0; j0 < ulen; j0 += 32) {
+            int j = j0 + lane;
+            if (j < ulen) {
+              uint64_t k1 = keys[ulo + j];
+              int w = (int)lkey_hub(k1);
+              int h1 = (int)lkey_hop(k1);
+              if (w != u && h1 <= h) {
+                const int32_t* rw = tab_find(T, mask, stride, w);
+                if (rw) {
+                  int32_t t = rw[1 + h - h1];
+                  if (t != kInf32) {
+                    long long c = (long long)lkey_dist(k1) + t;
+                    q = c < q ? c : q;
+                  }
+                }
+              }
+            }
+            if (__any_sync(0xffffffffu, q <= d)) break;
+          }
+          q = warp_min_ll(q);
+        }
+        keepit = !(q <= d);
+      }
+      if (lane == 0) keep[lo + i] = keepit ? 1 : 0;
+      my_kept += keepit ? 1 : 0;
+    }
+    if (lane == 0) s_kept[wid] = my_kept;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int64_t s = 0;
+      for (int i = 0; i < nw; i++) s += s_kept[i];
+      kept[v] = s;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint64_t* __restrict__ keys,
+                          const int32_t* __restrict__ par, const uint8_t* __restrict__ keep,
+                          const int64_t* __restrict__ noff, uint64_t* __restrict__ nkeys,
+                          int32_t* __restrict__ npar) {
+  const int lane = lane_id();
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = warp; v < n; v += nwarps) {
+    int64_t lo = off[v], len = off[v + 1] - lo, dst = noff[v];
+    for (int64_t j0 = 0; j0 < len; j0 += 32) {
+      int64_t j = j0 + lane;
+      bool k = j < len && keep[lo + j];
+      unsigned b = __ballot_sync(0xffffffffu, k);
+      if (k) {
+        int64_t at = dst + __popc(b & ((1u << lane) - 1));
+        nkeys[at] = keys[lo + j];
+        npar[at] = par[lo + j];
+      }
+      dst += __popc(b);
+    }
+  }
+}
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+int clean_index(hsdl_index_impl* idx) {
+  cudaStream_t st = idx->stream;
+  const int32_t n = idx->n, K = idx->K;
+  const int sms = device_sm_count();
+  const int stride = (K + 2 <= 8) ? 8 : 16;
+  double t0 = now_s();
+  // shared-memory table: up to 96 KB per block
+  const int smem_slots = (96 * 1024) / (stride * 4);
+  const size_t smem = (size_t)smem_slots * stride * 4;
+  HSDL_CUDA(cudaFuncSetAttribute(k_clean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t need_slots = 8;
+  while (need_slots < 2 * idx->max_row) need_slots <<= 1;
+  const int grid = sms * 2;
+  int64_t gslots = need_slots > smem_slots ? need_slots : 0;
+  DevBuf<int32_t> gscratch;
+  if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * stride));
+  DevBuf<uint8_t> keep;
+  DevBuf<int64_t> kept, noff;
+  DevBuf<int> next;
+  HSDL_TRY(keep.alloc(std::max<int64_t>(1, idx->total)));
+  HSDL_TRY(kept.alloc((int64_t)n + 1));
+  HSDL_TRY(noff.alloc((int64_t)n + 1));
+  HSDL_TRY(next.alloc(1));
+  HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
+  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->keys.p, keep.p, kept.p, stride, smem_slots,
+                                             gscratch.p, gslots, next.p);
+  HSDL_LAUNCHED();
+  HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
+  int64_t total = 0;
+  HSDL_CUDA(cudaMemcpyAsync(&total, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  DevBuf<uint64_t> nkeys;
+  DevBuf<int32_t> npar;
+  HSDL_TRY(nkeys.alloc(std::max<int64_t>(1, total)));
+  HSDL_TRY(npar.alloc(std::max<int64_t>(1, total)));
+  k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->keys.p, idx->par.p, keep.p, noff.p, nkeys.p, npar.p);
+  HSDL_LAUNCHED();
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  std::swap(idx->off.p, noff.p);
+  std::swap(idx->off.cap, noff.cap);
+  std::swap(idx->keys.p, nkeys.p);
+  std::swap(idx->keys.cap, nkeys.cap);
+  std::swap(idx->par.p, npar.p);
+  std::swap(idx->par.cap, npar.cap);
+  noff.release();
+  nkeys.release();
+  npar.release();
+  keep.release();
+  kept.release();
+  gscratch.release();
+  next.release();
+  idx->before = idx->total;
+  idx->total = total;
+  idx->after = total;
+  idx->cleaned = true;
+  idx->h_off.resize((size_t)n + 1);
+  HSDL_CUDA(cudaMemcpy(idx->h_off.data(), idx->off.p, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
+  int64_t mr = 0;
+  for (int32_t v = 0; v < n; v++) mr = std::max(mr, idx->h_off[v + 1] - idx->h_off[v]);
+  idx->max_row = mr;
+  idx->t_clean = now_s() - t0;
+  return HSDL_OK;
+}
+
+}  // namespace hsdl

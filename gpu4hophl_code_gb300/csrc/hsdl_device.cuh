@@ -1,0 +1,118 @@
+// Device-side helpers shared by the HSDL kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hsdl {
+
+// ---------------------------------------------------------------------------
+// Packed encodings.
+//
+// Label key (the per-vertex label store, 8 B):
+//     hub:28 | hop:4 | distance:32          (bits 63..36 | 35..32 | 31..0)
+// Unsigned order of the key is exactly the reference's label order
+// (hub asc, hop asc, distance asc; compare_hop_constrained_two_hop_label,
+// CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:373-387),
+// so sorting keys sorts labels.  parent_vertex is kept in a parallel int32
+// array.  Limits: vertex ids < 2^28 (the reference itself stops at 10^7,
+// generation.h:528-532), hop <= 14, distance < 2^31.
+//
+// Candidate key (per-slot search state, 8 B):
+//     distance:32 | hop:4 | parent:28
+// atomicMin on it keeps the smallest distance, then the smallest hop, then the
+// smallest predecessor id.  The all-ones value marks an untouched state (its
+// hop field, 15, is never a real hop).
+// ---------------------------------------------------------------------------
+constexpr uint64_t kEmptyCand = ~0ull;
+constexpr uint32_t kIdMask = (1u << 28) - 1;
+constexpr int32_t kMaxK = 14;
+constexpr int32_t kInf32 = 0x7F7F7F7F;  // "no value" in hub tables (memset 0x7F)
+constexpr int32_t kEmptyKey = 0x7F7F7F7F;
+
+__host__ __device__ inline uint64_t lkey(uint32_t hub, uint32_t hop, uint32_t dist) {
+  return ((uint64_t)hub << 36) | ((uint64_t)hop << 32) | (uint64_t)dist;
+}
+__host__ __device__ inline uint32_t lkey_hub(uint64_t k) { return (uint32_t)(k >> 36); }
+__host__ __device__ inline uint32_t lkey_hop(uint64_t k) { return (uint32_t)(k >> 32) & 15u; }
+__host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return (uint32_t)k; }
+
+__host__ __device__ inline uint64_t ckey(uint32_t dist, uint32_t hop, uint32_t parent) {
+  return ((uint64_t)dist << 32) | ((uint64_t)hop << 28) | (uint64_t)parent;
+}
+__host__ __device__ inline uint32_t ckey_dist(uint64_t k) { return (uint32_t)(k >> 32); }
+__host__ __device__ inline uint32_t ckey_hop(uint64_t k) { return (uint32_t)(k >> 28) & 15u; }
+__host__ __device__ inline uint32_t ckey_parent(uint64_t k) { return (uint32_t)k & kIdMask; }
+
+// Hub-table slot index for hub id w in a table of `mask+1` (power of two) slots.
+__device__ inline uint32_t table_hash(uint32_t w, uint32_t mask) {
+  uint32_t h = w * 2654435761u;
+  return (h ^ (h >> 15)) & mask;
+}
+
+// ---------------------------------------------------------------------------
+// Warp helpers.
+// ---------------------------------------------------------------------------
+__device__ inline int lane_id() { return threadIdx.x & 31; }
+
+__device__ inline long long warp_min_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  return v;
+}
+
+__device__ inline int64_t warp_sum_i64(int64_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Warp-aggregated append: every lane of the currently active mask with `pred`
+// gets a distinct slot from *counter; one atomic per warp.  Returns the slot
+// or -1 when pred is false.
+__device__ inline long long warp_append(bool pred, unsigned long long* counter) {
+  unsigned mask = __activemask();
+  unsigned ballot = __ballot_sync(mask, pred);
+  if (ballot == 0) return -1;
+  int leader = __ffs(ballot) - 1;
+  int lane = lane_id();
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(ballot));
+  base = __shfl_sync(mask, base, leader);
+  if (!pred) return -1;
+  return (long long)(base + __popc(ballot & ((1u << lane) - 1)));
+}
+
+// Block-wide exclusive scan of one int64 per thread (blockDim.x <= 1024,
+// multiple of 32).  `smem` must hold 32 int64.  Returns the exclusive prefix;
+// *total receives the block sum.
+__device__ inline int64_t block_exclusive_scan(int64_t v, int64_t* smem, int64_t* total) {
+  int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t s = lane < nw ? smem[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) smem[lane] = s;
+  }
+  __syncthreads();
+  int64_t warp_prefix = wid > 0 ? smem[wid - 1] : 0;
+  int64_t t = smem[nw - 1];
+  __syncthreads();
+  if (total) *total = t;
+  return warp_prefix + x - v;
+}
+
+}  // namespace hsdl

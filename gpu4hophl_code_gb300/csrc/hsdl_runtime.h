@@ -1,0 +1,123 @@
+// Host-side runtime shared by the CUDA translation units: handles, error
+// plumbing, device allocation with accounting, launch counting.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/hsdl.h"
+
+namespace hsdl {
+
+void set_error(const std::string& msg);
+std::atomic<int64_t>& launch_counter();
+
+// Status-returning error propagation.
+struct Status {
+  int code = HSDL_OK;
+  bool ok() const { return code == HSDL_OK; }
+};
+
+#define HSDL_CUDA(call)                                                                             \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      ::hsdl::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+      return (e_ == cudaErrorMemoryAllocation) ? HSDL_ERR_NOMEM : HSDL_ERR_CUDA;                    \
+    }                                                                                               \
+  } while (0)
+
+#define HSDL_TRY(expr)           \
+  do {                           \
+    int s_ = (expr);             \
+    if (s_ != HSDL_OK) return s_; \
+  } while (0)
+
+#define HSDL_LAUNCHED()                                            \
+  do {                                                             \
+    ::hsdl::launch_counter().fetch_add(1, std::memory_order_relaxed); \
+    cudaError_t e_ = cudaGetLastError();                           \
+    if (e_ != cudaSuccess) {                                       \
+      ::hsdl::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+      return HSDL_ERR_CUDA;                                        \
+    }                                                              \
+  } while (0)
+
+// A device buffer with accounting; grows by reallocation.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  int64_t cap = 0;  // elements
+  int alloc(int64_t n) {
+    release();
+    if (n <= 0) return HSDL_OK;
+    HSDL_CUDA(cudaMalloc(&p, (size_t)n * sizeof(T)));
+    cap = n;
+    return HSDL_OK;
+  }
+  // grows to at least n elements keeping the first `keep` elements
+  int grow(int64_t n, int64_t keep, cudaStream_t st) {
+    if (n <= cap) return HSDL_OK;
+    T* q = nullptr;
+    HSDL_CUDA(cudaMalloc(&q, (size_t)n * sizeof(T)));
+    if (keep > 0 && p) HSDL_CUDA(cudaMemcpyAsync(q, p, (size_t)keep * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    if (p) {
+      HSDL_CUDA(cudaStreamSynchronize(st));
+      cudaFree(p);
+    }
+    p = q;
+    cap = n;
+    return HSDL_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  int64_t bytes() const { return cap * (int64_t)sizeof(T); }
+};
+
+struct hsdl_graph_impl {
+  int32_t n = 0;
+  int64_t m2 = 0;
+  int32_t max_w = 0;
+  DevBuf<int64_t> rp;
+  DevBuf<int2> adj;  // (neighbour, weight)
+  std::vector<int64_t> h_rp;  // host copy of row_ptr (for sizing decisions)
+};
+
+// A built (or imported) label index resident in HBM.  Rows are sorted by the
+// packed label key; parents travel in a parallel array.
+struct hsdl_index_impl {
+  int32_t n = 0, K = 0;
+  bool cleaned = false;
+  DevBuf<int64_t> off;    // n+1
+  DevBuf<uint64_t> keys;  // label keys (hub:28 | hop:4 | dist:32)
+  DevBuf<int32_t> par;    // parent_vertex
+  int64_t total = 0;
+  int64_t before = 0, after = 0, max_row = 0;
+  int32_t waves = 0;
+  double t_gen = 0, t_sort = 0, t_clean = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<int64_t> h_off;  // host copy of offsets (path extraction, export)
+};
+
+int device_sm_count();
+int max_row_length(hsdl_index_impl* idx, int64_t* out);  // recomputes from h_off
+
+// kernels / stages implemented in the .cu files
+int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx);
+int clean_index(hsdl_index_impl* idx);
+int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
+                 int32_t* out, cudaStream_t st);
+int sort_rows(int32_t n, const int64_t* d_off, uint64_t* keys, int32_t* par, int64_t max_row, cudaStream_t st);
+int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total
+
+}  // namespace hsdl
+
+struct hsdl_graph : hsdl::hsdl_graph_impl {};
+struct hsdl_index : hsdl::hsdl_index_impl {};

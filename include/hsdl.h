@@ -1,0 +1,185 @@
+/*
+ * hsdl.h - C ABI of the GB300 hop-constrained shortest-distance 2-hop
+ * labeling (HSDL) engine: label generation, canonical clean and (s,t,k)
+ * distance queries on one GPU.
+ *
+ * Every function returns an int status (HSDL_OK = 0); on failure
+ * hsdl_last_error() returns a message for the calling thread.  Handles are
+ * opaque.  A handle may be used from one thread at a time; different handles
+ * may be used concurrently.  No torch or CUDA types appear in the signatures:
+ * streams are passed as `void*` (a cudaStream_t, NULL = the handle's own).
+ *
+ * Each entry point names the reference interface it replaces, as
+ * file:line inside the reference project (rucdatascience/GPU4HopHL_code).
+ *
+ * Limits (checked, HSDL_ERR_INVALID when exceeded): vertex count < 2^28,
+ * hop bound 1 <= K <= 14, edge weights >= 1 and K * max weight < 2^31.
+ */
+#ifndef HSDL_H
+#define HSDL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HSDL_OK 0
+#define HSDL_ERR_INVALID 1 /* bad argument or malformed input */
+#define HSDL_ERR_CUDA 2    /* CUDA runtime failure (no device, launch error) */
+#define HSDL_ERR_NOMEM 3   /* allocation failed or over the caller's budget */
+#define HSDL_ERR_TIMEOUT 4 /* a bounded device-side wait ran out */
+#define HSDL_ERR_STATE 5   /* call not valid in the handle's current state */
+#define HSDL_ERR_FULL 6    /* a queue or slot table is full */
+#define HSDL_ERR_IO 7      /* file could not be read or written */
+
+/* One label, byte-identical to the reference record
+ * hop_constrained_two_hop_label {hub_vertex, parent_vertex, hop, distance}
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:6-21). */
+typedef struct hsdl_label {
+  int32_t hub_vertex;
+  int32_t parent_vertex;
+  int32_t hop;
+  int32_t distance;
+} hsdl_label;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* hsdl_last_error(void);
+/* ABI version of this library. */
+int32_t hsdl_version(void);
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t hsdl_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Host graphs: seeded synthetic generators and loaders.  The result is an
+ * undirected simple graph relabelled by degree descending (ties: smaller
+ * original id first), as CSR rows sorted by neighbour id.  Replaces
+ * graph_v_of_v_update_vertexIDs_by_degrees_large_to_small
+ * (CPU_HopHL/include/graph_v_of_v/graph_v_of_v_update_vertexIDs_by_degrees_
+ * large_to_small.h:14-40, whose std::sort leaves ties unordered) and
+ * graph_v_of_v::txt_read (CPU_HopHL/include/graph_v_of_v/graph_v_of_v.h:242).
+ * ---------------------------------------------------------------------- */
+typedef struct hsdl_host_graph hsdl_host_graph;
+
+int hsdl_gen_erdos_renyi(int32_t n, int64_t m, int32_t wmin, int32_t wmax, uint64_t seed,
+                         hsdl_host_graph** out);
+int hsdl_gen_chung_lu(int32_t n, double avg_degree, double exponent, double max_degree, int32_t wmin,
+                      int32_t wmax, uint64_t seed, hsdl_host_graph** out);
+int hsdl_gen_barabasi_albert(int32_t n, int32_t m0, int32_t wmin, int32_t wmax, uint64_t seed,
+                             hsdl_host_graph** out);
+/* Undirected edge list (a[i], b[i], w[i]); rank_by_degree = 0 keeps ids. */
+int hsdl_host_graph_from_edges(int32_t n, int64_t m, const int32_t* a, const int32_t* b, const int32_t* w,
+                               int32_t rank_by_degree, hsdl_host_graph** out);
+/* graph_v_of_v text format ("|V|= n", "Edge a b w" lines). */
+int hsdl_read_graph_text(const char* path, int32_t rank_by_degree, hsdl_host_graph** out);
+/* Pointers stay valid until hsdl_host_graph_free.  new_to_old may be NULL. */
+int hsdl_host_graph_get(const hsdl_host_graph* g, int32_t* n, int64_t* adj_entries, const int64_t** row_ptr,
+                        const int32_t** col, const int32_t** w, const int32_t** new_to_old);
+void hsdl_host_graph_free(hsdl_host_graph* g);
+/* Checks the CSR form every device entry point requires. */
+int hsdl_validate_csr(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w);
+
+/* ------------------------------------------------------------------------
+ * Device graphs.  Copies a host CSR (ids = ranks, 0 highest) to HBM.  Plays
+ * the role of toCSR / graph_v_of_v_to_CSR + the managed-memory copy
+ * (Hybrid_Generation_Clean/include/graph/csr_graph.hpp:38,117).
+ * ---------------------------------------------------------------------- */
+typedef struct hsdl_graph hsdl_graph;
+
+int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w,
+                      hsdl_graph** out);
+int hsdl_graph_destroy(hsdl_graph* g);
+
+/* ------------------------------------------------------------------------
+ * Label generation.  Replaces hop_constrained_two_hop_labels_generation
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:513)
+ * and the GPU label_gen (Hybrid_Generation_Clean/src/label_gen.cu:603).
+ * Hubs are processed in rank order in waves; a wave's hubs see the labels of
+ * all earlier waves.  The result (before clean) is a superset of the
+ * canonical labels; with opts->clean = 1 the canonical set is returned.
+ * ---------------------------------------------------------------------- */
+typedef struct hsdl_build_opts {
+  int32_t struct_size;    /* sizeof(hsdl_build_opts) */
+  int32_t clean;          /* 1: run hsdl_clean after generation (default 1) */
+  int32_t first_wave;     /* hubs in the first wave (default 1) */
+  int32_t max_wave;       /* widest wave; waves double up to it (0 = auto) */
+  int32_t block_threads;  /* threads per block of the search kernels (0 = auto) */
+  int32_t frontier_tile;  /* frontier entries per expansion tile (0 = auto) */
+  int32_t prune_lanes;    /* lanes per candidate in the pruning join (0 = auto) */
+  int32_t reserved;
+  int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
+} hsdl_build_opts;
+
+void hsdl_build_opts_default(hsdl_build_opts* opts);
+/* Wave boundaries [b0=0, b1, ..., bW=n] the build uses for these options. */
+int hsdl_wave_bounds(int32_t n, const hsdl_build_opts* opts, int32_t* bounds, int32_t cap, int32_t* count);
+
+typedef struct hsdl_index hsdl_index;
+
+int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index** out);
+
+/* ------------------------------------------------------------------------
+ * Canonical repair.  Replaces hop_constrained_clean_L
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:422)
+ * and gpu_clean (Clean_mdnd/src/gpu_clean.cu:180,
+ * Hybrid_Generation_Clean/src/label_clean.cu:244).  Keeps label (u,h,d) of v
+ * iff no pair of labels through a hub ranked at or above u reaches v from u
+ * within h hops at distance <= d (the reference's rule, generation.h:451-482).
+ * ---------------------------------------------------------------------- */
+int hsdl_clean(hsdl_index* idx);
+
+/* ------------------------------------------------------------------------
+ * Queries.  Replace hop_constrained_extract_distance
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:144) and gpu_query
+ * (Query_mdnd/src/gpu_query.cu:84).  out[i] = min over common hubs of
+ * d1 + d2 with h1 + h2 <= k[i]; 0 if s == t; INT32_MAX if k < 1 (k < 0 or
+ * k == 0 with s != t) or if no pair exists.
+ * ---------------------------------------------------------------------- */
+int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
+                     int32_t* out);
+/* Same on device arrays, asynchronous on `stream`. */
+int hsdl_query_batch_device(hsdl_index* idx, int64_t nq, const int32_t* d_s, const int32_t* d_t,
+                            const int32_t* d_k, int32_t* d_out, void* stream);
+
+/* Path extraction: hop_constrained_extract_shortest_path
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:224).  Writes
+ * edges as (a,b) pairs into edges[2*cap]; *n_edges = count. */
+int hsdl_extract_path(hsdl_index* idx, int32_t s, int32_t t, int32_t k, int32_t* edges, int32_t cap,
+                      int32_t* n_edges);
+
+/* ------------------------------------------------------------------------
+ * Index contents.
+ * ---------------------------------------------------------------------- */
+typedef struct hsdl_index_info {
+  int32_t n;
+  int32_t K;
+  int32_t cleaned;               /* 1 after hsdl_clean */
+  int32_t waves;                 /* waves the generation ran */
+  int64_t labels;                /* current label count */
+  int64_t labels_before_clean;   /* label_size_before_canonical_repair */
+  int64_t labels_after_clean;    /* label_size_after_canonical_repair */
+  int64_t device_bytes;          /* HBM held by the index */
+  double time_generate_s;        /* time_generate_labels */
+  double time_sort_s;            /* time_sortL */
+  double time_clean_s;           /* time_canonical_repair */
+  int64_t max_row;               /* longest label list */
+} hsdl_index_info;
+
+int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);
+/* offsets[n+1], labels[offsets[n]]: each vertex's labels sorted by
+ * (hub, hop, distance), the reference's sortL order
+ * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:373-419). */
+int hsdl_export(hsdl_index* idx, int64_t* offsets, hsdl_label* labels);
+/* Builds an index from host labels (each row sorted as above). */
+int hsdl_import(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label* labels, hsdl_index** out);
+/* Binary label file of Clean_pc/main.cu:11-58 (save_labels / load_labels):
+ * size_t V; per vertex size_t count, then count x {hub, parent, hop, dist}. */
+int hsdl_save_labels(hsdl_index* idx, const char* path);
+int hsdl_load_labels(const char* path, int32_t K, hsdl_index** out);
+int hsdl_index_destroy(hsdl_index* idx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HSDL_H */

@@ -1,0 +1,195 @@
+"""ctypes wrapper of the HSDL oracle (test infrastructure only).
+
+Only the test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this module, as the checker / timed CPU baseline.  The
+product library never imports it.
+
+* ``Oracle``    - liboracle.so, this project's CPU restatement of the
+                  reference path (hsdl_oracle.cpp; every function cites the
+                  reference file:line it follows).
+* ``Reference`` - oracle/_ref/libhsdl_ref.so, the reference's own CPU_HopHL
+                  headers compiled in place (only where a reference checkout
+                  was available at build time).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libhsdl_ref.so")
+REF_DIR_DEFAULT = "/root/reference"
+
+
+def build(ref_dir: str | None = None) -> None:
+    """Compiles liboracle.so, and _ref/libhsdl_ref.so when the reference
+    checkout exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    ref_dir = ref_dir or os.environ.get("HSDL_REFERENCE_DIR", REF_DIR_DEFAULT)
+    if os.path.isdir(os.path.join(ref_dir, "CPU_HopHL", "include")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Labels:
+    """CPU label set: offsets int64[n+1], labels int32[total, 4]
+    (hub, parent, hop, distance)."""
+
+    def __init__(self, off: np.ndarray, lab: np.ndarray, info: dict | None = None):
+        self.off = off
+        self.lab = lab
+        self.info = info or {}
+
+    @property
+    def n(self):
+        return len(self.off) - 1
+
+    def row(self, v):
+        return self.lab[self.off[v]: self.off[v + 1]]
+
+
+class Oracle:
+    def __init__(self, path: str = PORT_LIB):
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+        L.orc_build.restype = vp
+        L.orc_build.argtypes = [i32, vp, vp, vp, i32, i32, vp, i32, i32]
+        L.orc_from_labels.restype = vp
+        L.orc_from_labels.argtypes = [i32, i32, vp, vp]
+        L.orc_clean.argtypes = [vp, i32, i32]
+        L.orc_size.restype = C.c_longlong
+        L.orc_size.argtypes = [vp]
+        L.orc_info.argtypes = [vp, vp, vp]
+        L.orc_export.argtypes = [vp, vp, vp]
+        L.orc_query.argtypes = [vp, i64, vp, vp, vp, vp, i32]
+        L.orc_path.restype = i32
+        L.orc_path.argtypes = [vp, i32, i32, i32, vp, i32]
+        L.orc_free.argtypes = [vp]
+        L.orc_bf.argtypes = [i32, vp, vp, vp, i32, i32, vp]
+        self.L = L
+
+    # -- handles -------------------------------------------------------------
+    def _export(self, h) -> Labels:
+        n = None
+        tot = self.L.orc_size(h)
+        info = np.zeros(6)
+        work = np.zeros(3, np.int64)
+        self.L.orc_info(h, _p(info), _p(work))
+        # n is recovered from export
+        off = np.zeros(self._n + 1, np.int64)
+        lab = np.zeros((max(1, tot), 4), np.int32)
+        self.L.orc_export(h, _p(off), _p(lab))
+        return Labels(off, lab[:tot], {"t_gen": info[0], "t_sort": info[1], "t_clean": info[2],
+                                       "before": int(info[3]), "after": int(info[4]),
+                                       "popped": int(work[0]), "relaxed": int(work[1]),
+                                       "query_reads": int(work[2])})
+
+    def build(self, g, K: int, threads: int = 1, wave_bounds=None, clean: bool = True) -> Labels:
+        """Generation (+ sortL, + clean).  wave_bounds: the GPU's wave schedule
+        (hsdl_wave_bounds) to reproduce its uncleaned superset exactly."""
+        b = None if wave_bounds is None else np.ascontiguousarray(wave_bounds, np.int32)
+        self._n = g.n
+        h = self.L.orc_build(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), K, threads, _p(b),
+                             0 if b is None else len(b), int(clean))
+        try:
+            return self._export(h)
+        finally:
+            self.L.orc_free(h)
+
+    def clean(self, labels: Labels, K: int, threads: int = 1, mode: int = 0) -> Labels:
+        """hop_constrained_clean_L on an arbitrary sorted label set."""
+        self._n = labels.n
+        lab = np.ascontiguousarray(labels.lab, np.int32)
+        h = self.L.orc_from_labels(labels.n, K, _p(labels.off), _p(lab))
+        try:
+            self.L.orc_clean(h, threads, mode)
+            return self._export(h)
+        finally:
+            self.L.orc_free(h)
+
+    def query(self, labels: Labels, s, t, k, threads: int = 1) -> np.ndarray:
+        self._n = labels.n
+        lab = np.ascontiguousarray(labels.lab, np.int32)
+        h = self.L.orc_from_labels(labels.n, 15, _p(labels.off), _p(lab))
+        try:
+            s = np.ascontiguousarray(s, np.int32)
+            t = np.ascontiguousarray(t, np.int32)
+            k = np.ascontiguousarray(k, np.int32)
+            out = np.zeros(len(s), np.int32)
+            self.L.orc_query(h, len(s), _p(s), _p(t), _p(k), _p(out), threads)
+            return out
+        finally:
+            self.L.orc_free(h)
+
+    def path(self, labels: Labels, s: int, t: int, k: int, cap: int = 64):
+        self._n = labels.n
+        lab = np.ascontiguousarray(labels.lab, np.int32)
+        h = self.L.orc_from_labels(labels.n, 15, _p(labels.off), _p(lab))
+        try:
+            e = np.zeros((cap, 2), np.int32)
+            c = self.L.orc_path(h, s, t, k, _p(e), cap)
+            return [tuple(x) for x in e[:max(c, 0)].tolist()]
+        finally:
+            self.L.orc_free(h)
+
+    def bf(self, g, src: int, k: int) -> np.ndarray:
+        out = np.zeros(g.n, np.int32)
+        self.L.orc_bf(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), src, k, _p(out))
+        return out
+
+
+class Reference:
+    """The reference's own CPU_HopHL (compiled from its headers in place)."""
+
+    available = os.path.exists(REF_LIB)
+
+    def __init__(self, path: str = REF_LIB):
+        L = C.CDLL(path)
+        vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+        L.ref_build.restype = C.c_int64
+        L.ref_build.argtypes = [i32, vp, vp, vp, i32, i32, i32]
+        L.ref_times.argtypes = [vp]
+        L.ref_export.argtypes = [vp, vp]
+        L.ref_query.argtypes = [i64, vp, vp, vp, vp, i32]
+        L.ref_bf.argtypes = [i32, i32, vp]
+        L.ref_path.restype = i32
+        L.ref_path.argtypes = [i32, i32, i32, vp, i32]
+        self.L = L
+        self.n = 0
+
+    def build(self, g, K: int, threads: int = 1, clean: bool = True) -> Labels:
+        tot = self.L.ref_build(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), K, threads, int(clean))
+        self.n = g.n
+        off = np.zeros(g.n + 1, np.int64)
+        lab = np.zeros((max(1, tot), 4), np.int32)
+        self.L.ref_export(_p(off), _p(lab))
+        t = np.zeros(4)
+        self.L.ref_times(_p(t))
+        return Labels(off, lab[:tot], {"t_init": t[0], "t_gen": t[1], "t_sort": t[2], "t_clean": t[3]})
+
+    def query(self, s, t, k, threads: int = 1) -> np.ndarray:
+        s = np.ascontiguousarray(s, np.int32)
+        t = np.ascontiguousarray(t, np.int32)
+        k = np.ascontiguousarray(k, np.int32)
+        out = np.zeros(len(s), np.int32)
+        self.L.ref_query(len(s), _p(s), _p(t), _p(k), _p(out), threads)
+        return out
+
+    def bf(self, src: int, k: int) -> np.ndarray:
+        out = np.zeros(self.n, np.int32)
+        self.L.ref_bf(src, k, _p(out))
+        return out
+
+    def path(self, s: int, t: int, k: int, cap: int = 64):
+        e = np.zeros((cap, 2), np.int32)
+        c = self.L.ref_path(s, t, k, _p(e), cap)
+        return [tuple(x) for x in e[:max(c, 0)].tolist()]

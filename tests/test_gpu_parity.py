@@ -1,0 +1,173 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden vectors.  Bit-exact on every integer field.
+
+* uncleaned GPU labels == oracle generation with the same wave schedule
+  (hub, parent, hop, distance - all four fields);
+* cleaned GPU labels == oracle sequential run (all four fields) and the
+  reference's labels (hub, hop, distance);
+* query answers == reference answers == hop-bounded Bellman-Ford.
+"""
+import numpy as np
+import pytest
+
+import gpu4hophl_code_gb300 as H
+
+pytestmark = pytest.mark.gpu
+
+INT_MAX = 2147483647
+
+
+def gpu_build(g, K, **opts):
+    dev = H.Graph(g)
+    idx = H.Index.build(dev, K, **opts)
+    return dev, idx
+
+
+def test_golden_cleaned_labels_and_queries(golden, orc):
+    g, K = golden.g, golden.K
+    dev, idx = gpu_build(g, K)
+    off, lab = idx.export()
+    ref = orc.build(g, K, threads=1)
+    assert np.array_equal(off, ref.off)
+    assert np.array_equal(lab, ref.lab)  # all four fields vs the oracle
+    if golden.full:
+        assert np.array_equal(lab[:, [0, 2, 3]], golden.d["labels"][:, [0, 2, 3]])
+    got = idx.query(golden.d["q_s"], golden.d["q_t"], golden.d["q_k"])
+    assert np.array_equal(got, golden.d["q_ans"])
+    for src, hop, bf in zip(golden.d["bf_src"], golden.d["bf_hop"], golden.d["bf_dist"]):
+        q = idx.query(np.full(g.n, src, np.int32), np.arange(g.n, dtype=np.int32), np.full(g.n, hop, np.int32))
+        assert np.array_equal(q, bf)
+
+
+@pytest.mark.parametrize("max_wave", [1, 4, 64, 0])
+def test_uncleaned_generation_matches_wave_oracle(orc, max_wave):
+    g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=21)
+    K = 5
+    dev, idx = gpu_build(g, K, clean=False, max_wave=max_wave)
+    b = H.wave_bounds(g.n, max_wave=max_wave)
+    off, lab = idx.export()
+    ref = orc.build(g, K, threads=4, wave_bounds=b, clean=False)
+    assert np.array_equal(off, ref.off)
+    assert np.array_equal(lab, ref.lab)
+    idx.clean()
+    off2, lab2 = idx.export()
+    canon = orc.build(g, K, threads=1)
+    assert np.array_equal(off2, canon.off) and np.array_equal(lab2, canon.lab)
+
+
+def test_gpu_clean_of_oracle_superset(orc):
+    """hsdl_clean on an imported superset equals the oracle's clean of it."""
+    g = H.HostGraph.erdos_renyi(800, 4000, 1, 50, seed=5)
+    K = 5
+    b = [0, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 800]
+    sup = orc.build(g, K, threads=4, wave_bounds=b, clean=False)
+    idx = H.Index.import_labels(g.n, K, sup.off, sup.lab)
+    idx.clean()
+    off, lab = idx.export()
+    canon = orc.build(g, K, threads=1)
+    assert np.array_equal(off, canon.off) and np.array_equal(lab, canon.lab)
+
+
+@pytest.mark.parametrize("kind,K", [("er", 1), ("er", 3), ("ba", 6), ("cl", 4), ("unit", 5), ("er", 9)])
+def test_graph_families_and_hop_bounds(orc, kind, K):
+    if kind == "er":
+        g = H.HostGraph.erdos_renyi(600, 2400, 1, 100, seed=K)
+    elif kind == "ba":
+        g = H.HostGraph.barabasi_albert(1500, 3, 1, 1000, seed=3)
+    elif kind == "cl":
+        g = H.HostGraph.chung_lu(5000, 10, 2.1, 500, 1, 100, seed=4)
+    else:
+        g = H.HostGraph.erdos_renyi(500, 1500, 1, 1, seed=6)  # unit weights: many ties
+    dev, idx = gpu_build(g, K)
+    off, lab = idx.export()
+    ref = orc.build(g, K, threads=1)
+    assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
+    rng = np.random.default_rng(K)
+    s = rng.integers(0, g.n, 20000).astype(np.int32)
+    t = rng.integers(0, g.n, 20000).astype(np.int32)
+    k = rng.integers(-1, K + 2, 20000).astype(np.int32)
+    assert np.array_equal(idx.query(s, t, k), orc.query(ref, s, t, k))
+
+
+def test_edge_cases_small_and_disconnected(orc):
+    # isolated vertices, two components, a path graph, n = 1
+    a = np.array([0, 1, 2, 5, 6], np.int32)
+    b = np.array([1, 2, 3, 6, 7], np.int32)
+    w = np.array([3, 1, 4, 1, 5], np.int32)
+    g = H.HostGraph.from_edges(10, a, b, w, rank_by_degree=True)
+    dev, idx = gpu_build(g, 3)
+    off, lab = idx.export()
+    ref = orc.build(g, 3, threads=1)
+    assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
+    s, t = np.meshgrid(np.arange(10, dtype=np.int32), np.arange(10, dtype=np.int32))
+    s, t = s.ravel(), t.ravel()
+    for k in (0, 1, 2, 3, 4):
+        kk = np.full(len(s), k, np.int32)
+        assert np.array_equal(idx.query(s, t, kk), orc.query(ref, s, t, kk))
+    one = H.HostGraph.from_edges(1, [], [], [], rank_by_degree=False)
+    d1, i1 = gpu_build(one, 2)
+    o1, l1 = i1.export()
+    assert list(o1) == [0, 1] and l1.tolist() == [[0, 0, 0, 0]]
+    assert list(i1.query([0], [0], [1])) == [0]
+
+
+def test_determinism_and_roundtrips(orc, tmp_path):
+    g = H.HostGraph.chung_lu(4000, 10, 2.1, 400, 1, 100, seed=77)
+    K = 5
+    _, a = gpu_build(g, K)
+    _, b = gpu_build(g, K)
+    oa, la = a.export()
+    ob, lb = b.export()
+    assert np.array_equal(oa, ob) and np.array_equal(la, lb)
+    c = H.Index.import_labels(g.n, K, oa, la)
+    oc, lc = c.export()
+    assert np.array_equal(oa, oc) and np.array_equal(la, lc)
+    p = str(tmp_path / "labels.bin")
+    a.save(p)
+    d = H.Index.load(p, K)
+    od, ld = d.export()
+    assert np.array_equal(oa, od) and np.array_equal(la, ld)
+    # file layout: size_t V, then per vertex size_t count + 16-byte records
+    raw = open(p, "rb").read()
+    assert int.from_bytes(raw[:8], "little") == g.n
+    assert len(raw) == 8 + 8 * g.n + 16 * len(la)
+
+
+def test_paths_are_valid_and_match_the_oracle(orc):
+    g = H.HostGraph.erdos_renyi(400, 1600, 1, 100, seed=9)
+    K = 5
+    _, idx = gpu_build(g, K)
+    ref = orc.build(g, K, threads=1)
+    rng = np.random.default_rng(1)
+    wmap = {}
+    for v in range(g.n):
+        for e in range(g.row_ptr[v], g.row_ptr[v + 1]):
+            wmap[(v, int(g.col[e]))] = int(g.w[e])
+    for _ in range(200):
+        s, t, k = int(rng.integers(g.n)), int(rng.integers(g.n)), int(rng.integers(1, K + 1))
+        p = idx.path(s, t, k)
+        assert p == orc.path(ref, s, t, k)
+        d = int(idx.query([s], [t], [k])[0])
+        if s == t:
+            assert p == []
+        elif d == INT_MAX:
+            assert p == []
+        else:
+            assert sum(wmap[(a, b)] for a, b in p) == d and len(p) <= k
+
+
+def test_reference_shaped_api(orc):
+    g = H.HostGraph.erdos_renyi(300, 1200, 1, 100, seed=2)
+    ci = H.hop_constrained_case_info(upper_k=4, use_canonical_repair=True, thread_num=8)
+    H.hop_constrained_two_hop_labels_generation(g, ci)
+    ref = orc.build(g, 4, threads=1)
+    assert ci.L.total() == len(ref.lab)
+    assert ci.label_size_after_canonical_repair == len(ref.lab)
+    assert ci.label_size_before_canonical_repair >= ci.label_size_after_canonical_repair
+    for v in (0, 5, 299):
+        assert np.array_equal(ci.L[v], ref.row(v))
+    assert H.hop_constrained_extract_distance(ci.L, 3, 3, 2) == 0
+    assert H.hop_constrained_extract_distance(ci.L, 3, 7, -1) == INT_MAX
+    q = np.array([[1, 2, 3], [4, 5, 4], [7, 7, 0]], np.int32)
+    ans, secs = H.gpu_query(ci.L, q, 4)
+    assert np.array_equal(ans, orc.query(ref, q[:, 0], q[:, 1], q[:, 2]))
