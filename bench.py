@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""HSDL benchmark on the 1M-vertex power-law graph (hop bound K = 5).
+
+Workload: seeded Chung-Lu graph, n = 1,000,000, average degree 10, degree
+exponent 2.1, maximum expected degree 10,000, int32 weights uniform [1, 100],
+vertices ranked by degree (ties by id); label generation + canonical clean on
+the GPU, then batches of 10,000,000 uniform (s, t, k) queries, k uniform in
+[1, 5].  A step is one batch of queries over the resident index.
+
+value  - queries/s of the batched query kernel with queries and labels already
+         in HBM (CUDA events on the launching stream).
+e2e    - the same metric through the C ABI call hsdl_query_batch with host
+         (pinned) buffers: host->device copy of the queries and device->host
+         copy of the answers inside the timed region.
+build  - generation + clean seconds and labels/s, reported beside the metric.
+
+--impl reference times the reference's CPU query path
+(hop_constrained_extract_distance, restated in oracle/) on all host cores over
+the same labels, and prints the same JSON line with "impl": "reference".
+
+Multi-GPU (torchrun, N ranks): replicas only - every rank builds its own index
+and answers its own query batches; value = all ranks' queries / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 0x48534C44 ^ 2
+METRIC = "serving queries/s & p99 us vs plain path, exact, 1M-vert graph K=5; build s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--queries", type=int, default=10_000_000)
+    ap.add_argument("--K", type=int, default=5)
+    ap.add_argument("--cpu-baseline-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[0]) for r in rows if r[0].strip().replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for i, nm in enumerate(names):
+                if len(r) > 4 + i and r[4 + i].strip() == "Active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def make_graph(n):
+    import gpu4hophl_code_gb300 as H
+
+    return H.HostGraph.chung_lu(n, 10.0, 2.1, 10000.0, 1, 100, seed=SEED)
+
+
+def make_queries(n, nq, K, seed):
+    rng = np.random.default_rng(seed)
+    s = rng.integers(0, n, nq, dtype=np.int32)
+    t = rng.integers(0, n, nq, dtype=np.int32)
+    k = rng.integers(1, K + 1, nq, dtype=np.int32)
+    return s, t, k
+
+
+def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
+    """Per query: the two label rows as packed 8-byte keys (hub:28|hop:4|
+    distance:32), the four row offsets (32 B), the (s,t,k) record in (12 B)
+    and the answer out (4 B)."""
+    ln = np.diff(off)
+    rows = ln[s].astype(np.int64) + ln[t].astype(np.int64)
+    rows[s == t] = 0
+    return int(8 * rows.sum() + 48 * len(s))
+
+
+def cpu_query_baseline(off, lab, s, t, k, seconds, threads):
+    """Reference query path (hop_constrained_extract_distance restated in
+    oracle/) over a bounded sample of the batch, on `threads` host cores."""
+    from oracle.oracle import Labels, Oracle
+
+    O = Oracle()
+    L = Labels(off, lab)
+    # warm and size the sample to about `seconds` of CPU time
+    m = 20000
+    t0 = time.perf_counter()
+    O.query(L, s[:m], t[:m], k[:m], threads=threads)
+    dt = max(1e-6, time.perf_counter() - t0)
+    m2 = int(min(len(s), max(m, m * seconds / dt)))
+    t0 = time.perf_counter()
+    out = O.query(L, s[:m2], t[:m2], k[:m2], threads=threads)
+    dt = time.perf_counter() - t0
+    return m2 / dt, m2, dt, out
+
+
+def init_dist(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return dist, rank, world, local
+    return None, 0, 1, 0
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args, dist, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    import gpu4hophl_code_gb300 as H
+    from gpu4hophl_code_gb300 import _native
+
+    L = _native.lib()
+    g = make_graph(args.n)
+    dev = H.Graph(g)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = H.Index.build(dev, args.K, clean=True)
+    build_s = time.perf_counter() - t0
+    info = idx.info()
+
+    s, t, k = make_queries(args.n, args.queries, args.K, seed=1000 + rank)
+    stream = torch.cuda.Stream()
+    ds = torch.from_numpy(s).to("cuda")
+    dt_ = torch.from_numpy(t).to("cuda")
+    dk = torch.from_numpy(k).to("cuda")
+    dout = torch.empty(args.queries, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def step():
+        idx.query_device(args.queries, ds.data_ptr(), dt_.data_ptr(), dk.data_ptr(), dout.data_ptr(),
+                         stream=stream.cuda_stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = L.hsdl_launch_count()
+    barrier(dist)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches = L.hsdl_launch_count() - launches0
+    kernel_ms = ev0.elapsed_time(ev1)
+    t_max = max_over_ranks(dist, kernel_ms / 1000.0)
+    value = world * args.queries * args.steps / t_max
+    answers = dout.cpu().numpy()
+
+    # end to end through the C ABI with pinned host buffers
+    hs = torch.from_numpy(s).pin_memory()
+    ht = torch.from_numpy(t).pin_memory()
+    hk = torch.from_numpy(k).pin_memory()
+    ho = torch.empty(args.queries, dtype=torch.int32).pin_memory()
+    P = lambda x: x.data_ptr()  # noqa: E731
+    for _ in range(2):
+        _native.check(L.hsdl_query_batch(idx.handle, args.queries, P(hs), P(ht), P(hk), P(ho)))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _native.check(L.hsdl_query_batch(idx.handle, args.queries, P(hs), P(ht), P(hk), P(ho)))
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    clk = clocks.stop()
+    e2e = world * args.queries * args.steps / e2e_s
+    assert np.array_equal(ho.numpy(), answers), "e2e answers differ from the device-path answers"
+
+    # roofline of the query kernel
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    res = {}
+    if rank == 0:
+        off, lab = idx.export()
+        bytes_per_launch = algorithmic_bytes(off, s, t, k)
+        achieved = bytes_per_launch / (kernel_ms / 1000.0 / args.steps) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                "traffic": None,
+                "kernel": "k_query", "algorithmic_bytes_per_launch": bytes_per_launch,
+                "bytes_per_query": round(bytes_per_launch / args.queries, 1)}
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            qps, m2, secs, out = cpu_query_baseline(off, lab, s, t, k, args.cpu_baseline_seconds, threads)
+            assert np.array_equal(out, answers[:m2]), "CPU baseline answers differ from the GPU's"
+            cpu = {"value": round(qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+                   "sample": f"{m2} of the batch's {args.queries} queries over the same 1M-vertex labels "
+                             f"({secs:.1f} s), oracle restatement of hop_constrained_extract_distance"}
+        res = {
+            "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": round(t_max * 1000.0 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded Chung-Lu graph and uniform queries)",
+            "config": {"workload": f"chung_lu n={args.n} avg_deg=10 gamma=2.1 max_deg=10000 w=[1,100] K={args.K}; "
+                                   f"{args.queries} uniform (s,t,k) queries per step, k in [1,{args.K}]",
+                       "n": args.n, "K": args.K, "queries_per_step": args.queries,
+                       "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (label index "
+                             f"{info['device_bytes'] / 1e9:.1f} GB)"},
+            "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": 12 * args.queries,
+                    "d2h_bytes_per_step": 4 * args.queries},
+            "build": {"seconds": round(build_s, 3), "generate_s": round(info["time_generate_s"], 3),
+                      "sort_s": round(info["time_sort_s"], 3), "clean_s": round(info["time_clean_s"], 3),
+                      "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
+                      "labels_per_s": round(info["labels"] / build_s, 1), "waves": info["waves"]},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }
+    return res
+
+
+def run_reference(args, dist, rank, world, local):
+    """The reference's CPU query path on all host cores over the same labels.
+    The labels are the canonical set (bit-identical to CPU_HopHL's output for
+    this order and K); they are produced once on the GPU as untimed input
+    because the CPU build of a 1M-vertex index takes tens of minutes."""
+    if rank != 0:
+        return None
+    import torch
+
+    torch.cuda.set_device(local)
+    import gpu4hophl_code_gb300 as H
+
+    g = make_graph(args.n)
+    dev = H.Graph(g)
+    idx = H.Index.build(dev, args.K, clean=True)
+    off, lab = idx.export()
+    idx.close()
+    dev.close()
+    s, t, k = make_queries(args.n, args.queries, args.K, seed=1000)
+    from oracle.oracle import Labels, Oracle
+
+    O = Oracle()
+    Lb = Labels(off, lab)
+    threads = os.cpu_count() or 1
+    per_step = max(20000, min(args.queries, 2_000_000))
+    for i in range(max(1, args.warmup)):
+        O.query(Lb, s[:20000], t[:20000], k[:20000], threads=threads)
+    t0 = time.perf_counter()
+    done = 0
+    for i in range(args.steps):
+        lo = (i * per_step) % max(1, args.queries - per_step + 1)
+        O.query(Lb, s[lo:lo + per_step], t[lo:lo + per_step], k[lo:lo + per_step], threads=threads)
+        done += per_step
+    secs = time.perf_counter() - t0
+    v = done / secs
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1000 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded Chung-Lu graph and uniform queries)",
+            "config": {"workload": f"chung_lu n={args.n} avg_deg=10 gamma=2.1 max_deg=10000 w=[1,100] K={args.K}; "
+                                   f"uniform (s,t,k) queries, k in [1,{args.K}]",
+                       "n": args.n, "K": args.K, "queries_per_step": per_step, "parallelism": "cpu"},
+            "cpu_baseline": {"value": round(v, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} queries per step over the 1M-vertex canonical labels"},
+            "e2e": {"value": round(v, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    dist, rank, world, local = init_dist(args)
+    if args.impl == "reference":
+        res = run_reference(args, dist, rank, world, local)
+    else:
+        res = run_ours(args, dist, rank, world, local)
+    if rank == 0 and res:
+        print(json.dumps(res), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
