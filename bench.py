@@ -123,20 +123,19 @@ def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
 
 def cpu_query_baseline(off, lab, s, t, k, seconds, threads):
     """Reference query path (hop_constrained_extract_distance restated in
-    oracle/) over a bounded sample of the batch, on `threads` host cores."""
+    oracle/) over a bounded sample of the batch, on `threads` host cores.
+    The label set is loaded into the oracle once, outside the timed region."""
     from oracle.oracle import Labels, Oracle
 
-    O = Oracle()
-    L = Labels(off, lab)
-    # warm and size the sample to about `seconds` of CPU time
-    m = 20000
-    t0 = time.perf_counter()
-    O.query(L, s[:m], t[:m], k[:m], threads=threads)
-    dt = max(1e-6, time.perf_counter() - t0)
-    m2 = int(min(len(s), max(m, m * seconds / dt)))
-    t0 = time.perf_counter()
-    out = O.query(L, s[:m2], t[:m2], k[:m2], threads=threads)
-    dt = time.perf_counter() - t0
+    with Oracle().index(Labels(off, lab)) as ix:
+        m = 50000
+        t0 = time.perf_counter()
+        ix.query(s[:m], t[:m], k[:m], threads=threads)
+        dt = max(1e-6, time.perf_counter() - t0)
+        m2 = int(min(len(s), max(m, m * seconds / dt)))
+        t0 = time.perf_counter()
+        out = ix.query(s[:m2], t[:m2], k[:m2], threads=threads)
+        dt = time.perf_counter() - t0
     return m2 / dt, m2, dt, out
 
 
@@ -306,19 +305,19 @@ def run_reference(args, dist, rank, world, local):
     s, t, k = make_queries(args.n, args.queries, args.K, seed=1000)
     from oracle.oracle import Labels, Oracle
 
-    O = Oracle()
-    Lb = Labels(off, lab)
+    ix = Oracle().index(Labels(off, lab))  # label conversion is setup, not timed
     threads = os.cpu_count() or 1
-    per_step = max(20000, min(args.queries, 2_000_000))
+    per_step = max(50000, min(args.queries, 4_000_000))
     for i in range(max(1, args.warmup)):
-        O.query(Lb, s[:20000], t[:20000], k[:20000], threads=threads)
+        ix.query(s[:50000], t[:50000], k[:50000], threads=threads)
     t0 = time.perf_counter()
     done = 0
     for i in range(args.steps):
         lo = (i * per_step) % max(1, args.queries - per_step + 1)
-        O.query(Lb, s[lo:lo + per_step], t[lo:lo + per_step], k[lo:lo + per_step], threads=threads)
+        ix.query(s[lo:lo + per_step], t[lo:lo + per_step], k[lo:lo + per_step], threads=threads)
         done += per_step
     secs = time.perf_counter() - t0
+    ix.close()
     v = done / secs
     return {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "queries/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1000 / args.steps, 3),

@@ -116,30 +116,17 @@ class Oracle:
         finally:
             self.L.orc_free(h)
 
+    def index(self, labels: Labels) -> "OracleIndex":
+        """Loads a label set once; queries and paths then run on it."""
+        return OracleIndex(self, labels)
+
     def query(self, labels: Labels, s, t, k, threads: int = 1) -> np.ndarray:
-        self._n = labels.n
-        lab = np.ascontiguousarray(labels.lab, np.int32)
-        h = self.L.orc_from_labels(labels.n, 15, _p(labels.off), _p(lab))
-        try:
-            s = np.ascontiguousarray(s, np.int32)
-            t = np.ascontiguousarray(t, np.int32)
-            k = np.ascontiguousarray(k, np.int32)
-            out = np.zeros(len(s), np.int32)
-            self.L.orc_query(h, len(s), _p(s), _p(t), _p(k), _p(out), threads)
-            return out
-        finally:
-            self.L.orc_free(h)
+        with self.index(labels) as ix:
+            return ix.query(s, t, k, threads)
 
     def path(self, labels: Labels, s: int, t: int, k: int, cap: int = 64):
-        self._n = labels.n
-        lab = np.ascontiguousarray(labels.lab, np.int32)
-        h = self.L.orc_from_labels(labels.n, 15, _p(labels.off), _p(lab))
-        try:
-            e = np.zeros((cap, 2), np.int32)
-            c = self.L.orc_path(h, s, t, k, _p(e), cap)
-            return [tuple(x) for x in e[:max(c, 0)].tolist()]
-        finally:
-            self.L.orc_free(h)
+        with self.index(labels) as ix:
+            return ix.path(s, t, k, cap)
 
     def bf(self, g, src: int, k: int) -> np.ndarray:
         out = np.zeros(g.n, np.int32)
@@ -193,3 +180,42 @@ class Reference:
         e = np.zeros((cap, 2), np.int32)
         c = self.L.ref_path(s, t, k, _p(e), cap)
         return [tuple(x) for x in e[:max(c, 0)].tolist()]
+
+
+class OracleIndex:
+    """A label set loaded into the oracle (conversion paid once)."""
+
+    def __init__(self, orc: Oracle, labels: Labels):
+        self.L = orc.L
+        lab = np.ascontiguousarray(labels.lab, np.int32)
+        self.h = self.L.orc_from_labels(labels.n, 15, _p(labels.off), _p(lab))
+
+    def query(self, s, t, k, threads: int = 1) -> np.ndarray:
+        s = np.ascontiguousarray(s, np.int32)
+        t = np.ascontiguousarray(t, np.int32)
+        k = np.ascontiguousarray(k, np.int32)
+        out = np.zeros(len(s), np.int32)
+        self.L.orc_query(self.h, len(s), _p(s), _p(t), _p(k), _p(out), threads)
+        return out
+
+    def path(self, s: int, t: int, k: int, cap: int = 64):
+        e = np.zeros((cap, 2), np.int32)
+        c = self.L.orc_path(self.h, s, t, k, _p(e), cap)
+        return [tuple(x) for x in e[:max(c, 0)].tolist()]
+
+    def close(self):
+        if self.h:
+            self.L.orc_free(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
