@@ -74,6 +74,7 @@ SIGNATURES = {
     "hsdl_clean": (C.c_int, [P]),
     "hsdl_query_batch": (C.c_int, [P, I64, P, P, P, P]),
     "hsdl_query_batch_device": (C.c_int, [P, I64, P, P, P, P, P]),
+    "hsdl_query_batch_static": (C.c_int, [P, I64, P, P, P, P]),
     "hsdl_extract_path": (C.c_int, [P, I32, I32, I32, P, I32, C.POINTER(I32)]),
     "hsdl_index_get_info": (C.c_int, [P, C.POINTER(hsdl_index_info)]),
     "hsdl_export": (C.c_int, [P, P, P]),

@@ -132,14 +132,30 @@ int hsdl_clean(hsdl_index* idx);
  * Queries.  Replace hop_constrained_extract_distance
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:144) and gpu_query
  * (Query_mdnd/src/gpu_query.cu:84).  out[i] = min over common hubs of
- * d1 + d2 with h1 + h2 <= k[i]; 0 if s == t; INT32_MAX if k < 1 (k < 0 or
- * k == 0 with s != t) or if no pair exists.
+ * d1 + d2 with h1 + h2 <= k[i], INT32_MAX if no pair exists; checked first,
+ * as in the reference: k < 0 -> INT32_MAX, then s == t -> 0, then
+ * k == 0 -> INT32_MAX.
  * ---------------------------------------------------------------------- */
 int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                      int32_t* out);
 /* Same on device arrays, asynchronous on `stream`. */
 int hsdl_query_batch_device(hsdl_index* idx, int64_t nq, const int32_t* d_s, const int32_t* d_t,
                             const int32_t* d_k, int32_t* d_out, void* stream);
+
+/* Same as hsdl_query_batch, but allocates no device memory: the queries and
+ * answers are staged in one fixed-size device array inside the library
+ * instead of per-call allocations.  For callers that cannot allocate device
+ * memory - next to running serving or build kernels (cudaMalloc/cudaFree can
+ * synchronise the device), under another allocator's hard cap, or while a
+ * CUDA graph is captured in global mode.  This entry point has no counterpart
+ * in the reference.  At most HSDL_STATIC_QUERY_MAX queries per call (larger
+ * batches: HSDL_ERR_INVALID).  The array (16 MiB) is held by every GPU that
+ * loads the library until exit; the first call on a device looks up its
+ * address, so make it before any stream capture.  Calls share the array and
+ * are serialised by a process-wide lock (overlapping calls would race). */
+#define HSDL_STATIC_QUERY_MAX (1 << 20)
+int hsdl_query_batch_static(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
+                            int32_t* out);
 
 /* Path extraction: hop_constrained_extract_shortest_path
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:224).  Writes
