@@ -112,13 +112,14 @@ def make_queries(n, nq, K, seed):
 
 
 def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
-    """Per query: the two label rows as packed 8-byte keys (hub:28|hop:4|
-    distance:32), the four row offsets (32 B), the (s,t,k) record in (12 B)
-    and the answer out (4 B)."""
+    """Per query: the hub ids of both label rows (4 B each; the join must read
+    every one), the four row offsets (32 B), the (s,t,k) record in (12 B) and
+    the answer out (4 B).  The hop/distance words read on hub matches are not
+    counted, so the achieved bandwidth derived from this is a lower bound."""
     ln = np.diff(off)
     rows = ln[s].astype(np.int64) + ln[t].astype(np.int64)
     rows[s == t] = 0
-    return int(8 * rows.sum() + 48 * len(s))
+    return int(4 * rows.sum() + 48 * len(s))
 
 
 def cpu_query_baseline(off, lab, s, t, k, seconds, threads):

@@ -84,20 +84,25 @@ void free_index(hsdl_index* idx) {
   if (!idx) return;
   if (idx->stream) cudaStreamSynchronize(idx->stream);
   idx->off.release();
-  idx->keys.release();
+  idx->hub.release();
+  idx->hd.release();
   idx->par.release();
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;
 }
 
-// Copies rows [v] of an index to the host (keys + parents).
+// Copies row v of an index to the host as packed keys (hub << 32 | hd) and
+// parents.
 int fetch_row(hsdl_index* idx, int32_t v, std::vector<uint64_t>& k, std::vector<int32_t>& p) {
   int64_t lo = idx->h_off[v], len = idx->h_off[v + 1] - lo;
   k.resize(len);
   p.resize(len);
   if (len == 0) return HSDL_OK;
-  HSDL_CUDA(cudaMemcpy(k.data(), idx->keys.p + lo, len * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> hb(len), hd(len);
+  HSDL_CUDA(cudaMemcpy(hb.data(), idx->hub.p + lo, len * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  HSDL_CUDA(cudaMemcpy(hd.data(), idx->hd.p + lo, len * sizeof(uint32_t), cudaMemcpyDeviceToHost));
   HSDL_CUDA(cudaMemcpy(p.data(), idx->par.p + lo, len * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < len; i++) k[i] = ((uint64_t)hb[i] << 32) | hd[i];
   return HSDL_OK;
 }
 
@@ -106,20 +111,25 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
   HSDL_CHECK_ARG(offsets && offsets[0] == 0, "offsets[0] must be 0");
   int64_t total = offsets[n];
-  std::vector<uint64_t> keys((size_t)total);
+  std::vector<uint32_t> hub((size_t)total), hd((size_t)total);
   std::vector<int32_t> par((size_t)total);
   int64_t mr = 0;
   for (int32_t v = 0; v < n; v++) {
     HSDL_CHECK_ARG(offsets[v + 1] >= offsets[v], "offsets must be non-decreasing");
     mr = std::max(mr, offsets[v + 1] - offsets[v]);
+    uint64_t prev = 0;
     for (int64_t i = offsets[v]; i < offsets[v + 1]; i++) {
       const hsdl_label& x = labels[i];
-      HSDL_CHECK_ARG(x.hub_vertex >= 0 && x.hub_vertex < n && x.hop >= 0 && x.hop <= K && x.distance >= 0,
+      HSDL_CHECK_ARG(x.hub_vertex >= 0 && x.hub_vertex < n && x.hop >= 0 && x.hop <= K && x.distance >= 0 &&
+                         (uint32_t)x.distance <= kDistMask,
                      "label field out of range at entry " + std::to_string(i));
-      keys[i] = lkey((uint32_t)x.hub_vertex, (uint32_t)x.hop, (uint32_t)x.distance);
-      par[i] = x.parent_vertex;
-      HSDL_CHECK_ARG(i == offsets[v] || keys[i - 1] < keys[i],
+      uint64_t key = lkey((uint32_t)x.hub_vertex, (uint32_t)x.hop, (uint32_t)x.distance);
+      HSDL_CHECK_ARG(i == offsets[v] || prev < key,
                      "row " + std::to_string(v) + " is not sorted by (hub, hop, distance)");
+      prev = key;
+      hub[i] = lkey_hub(key);
+      hd[i] = lkey_hd(key);
+      par[i] = x.parent_vertex;
     }
   }
   idx->n = n;
@@ -128,11 +138,13 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   idx->before = idx->after = total;
   idx->max_row = mr;
   HSDL_TRY(idx->off.alloc((int64_t)n + 1));
-  HSDL_TRY(idx->keys.alloc(std::max<int64_t>(1, total)));
-  HSDL_TRY(idx->par.alloc(std::max<int64_t>(1, total)));
+  HSDL_TRY(idx->hub.alloc(total + kRowPad));
+  HSDL_TRY(idx->hd.alloc(total + kRowPad));
+  HSDL_TRY(idx->par.alloc(total + kRowPad));
   HSDL_CUDA(cudaMemcpy(idx->off.p, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice));
   if (total > 0) {
-    HSDL_CUDA(cudaMemcpy(idx->keys.p, keys.data(), sizeof(uint64_t) * total, cudaMemcpyHostToDevice));
+    HSDL_CUDA(cudaMemcpy(idx->hub.p, hub.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
+    HSDL_CUDA(cudaMemcpy(idx->hd.p, hd.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
     HSDL_CUDA(cudaMemcpy(idx->par.p, par.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice));
   }
   idx->h_off.assign(offsets, offsets + n + 1);
@@ -355,7 +367,7 @@ int hsdl_wave_bounds(int32_t n, const hsdl_build_opts* opts, int32_t* bounds, in
 int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index** out) {
   HSDL_CHECK_ARG(g && out, "null argument");
   HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
-  HSDL_CHECK_ARG((int64_t)K * g->max_w < (int64_t)INT32_MAX, "K * max edge weight must be < 2^31");
+  HSDL_CHECK_ARG((int64_t)K * g->max_w <= (int64_t)kDistMask, "K * max edge weight must be < 2^28");
   hsdl_build_opts o;
   HSDL_TRY(resolve_opts(opts, &o));
   hsdl_index* idx = nullptr;
@@ -489,7 +501,7 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->labels = idx->total;
   info->labels_before_clean = idx->before;
   info->labels_after_clean = idx->after;
-  info->device_bytes = idx->off.bytes() + idx->keys.bytes() + idx->par.bytes();
+  info->device_bytes = idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
   info->time_generate_s = idx->t_gen;
   info->time_sort_s = idx->t_sort;
   info->time_clean_s = idx->t_clean;
@@ -500,18 +512,19 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
 int hsdl_export(hsdl_index* idx, int64_t* offsets, hsdl_label* labels) {
   HSDL_CHECK_ARG(idx && offsets && (idx->total == 0 || labels), "null argument");
   HSDL_CUDA(cudaStreamSynchronize(idx->stream));
-  std::vector<uint64_t> keys((size_t)idx->total);
+  std::vector<uint32_t> hub((size_t)idx->total), hd((size_t)idx->total);
   std::vector<int32_t> par((size_t)idx->total);
   if (idx->total > 0) {
-    HSDL_CUDA(cudaMemcpy(keys.data(), idx->keys.p, sizeof(uint64_t) * idx->total, cudaMemcpyDeviceToHost));
+    HSDL_CUDA(cudaMemcpy(hub.data(), idx->hub.p, sizeof(uint32_t) * idx->total, cudaMemcpyDeviceToHost));
+    HSDL_CUDA(cudaMemcpy(hd.data(), idx->hd.p, sizeof(uint32_t) * idx->total, cudaMemcpyDeviceToHost));
     HSDL_CUDA(cudaMemcpy(par.data(), idx->par.p, sizeof(int32_t) * idx->total, cudaMemcpyDeviceToHost));
   }
   std::copy(idx->h_off.begin(), idx->h_off.end(), offsets);
   for (int64_t i = 0; i < idx->total; i++) {
-    labels[i].hub_vertex = (int32_t)lkey_hub(keys[i]);
+    labels[i].hub_vertex = (int32_t)hub[i];
     labels[i].parent_vertex = par[i];
-    labels[i].hop = (int32_t)lkey_hop(keys[i]);
-    labels[i].distance = (int32_t)lkey_dist(keys[i]);
+    labels[i].hop = (int32_t)hd_hop(hd[i]);
+    labels[i].distance = (int32_t)hd_dist(hd[i]);
   }
   return HSDL_OK;
 }

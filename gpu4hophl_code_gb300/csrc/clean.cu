@@ -47,7 +47,8 @@ __device__ inline const int32_t* tab_find(const int32_t* T, uint32_t mask, int s
 }
 
 __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, const int64_t* __restrict__ off,
-                                                         const uint64_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ hub,
+                                                         const uint32_t* __restrict__ hd,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
                                                          int stride, int smem_slots, int32_t* __restrict__ gscratch,
                                                          int64_t gscratch_slots, int* __restrict__ next_v) {
@@ -69,8 +70,8 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
     for (int64_t i = threadIdx.x; i < cap * stride; i += blockDim.x) T[i] = kInf32;
     __syncthreads();
     for (int j = threadIdx.x; j < len; j += blockDim.x) {
-      uint64_t k = keys[lo + j];
-      int32_t w = (int32_t)lkey_hub(k);
+      int32_t w = (int32_t)hub[lo + j];
+      uint32_t x = hd[lo + j];
       uint32_t ix = table_hash((uint32_t)w, mask);
       bool placed = false;
       for (uint32_t probe = 0; probe <= mask; probe++) {  // the table is at most half full
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
         }
         ix = (ix + 1) & mask;
       }
-      if (placed) atomicMin(&T[(int64_t)ix * stride + 1 + lkey_hop(k)], (int32_t)lkey_dist(k));
+      if (placed) atomicMin(&T[(int64_t)ix * stride + 1 + hd_hop(x)], (int32_t)hd_dist(x));
     }
     __syncthreads();
     for (int64_t e = threadIdx.x; e < cap; e += blockDim.x) {
@@ -96,10 +97,10 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
     __syncthreads();
     int my_kept = 0;
     for (int i = wid; i < len; i += nw) {
-      uint64_t k = keys[lo + i];
-      int u = (int)lkey_hub(k);
-      int h = (int)lkey_hop(k);
-      long long d = (long long)lkey_dist(k);
+      int u = (int)hub[lo + i];
+      uint32_t x = hd[lo + i];
+      int h = (int)hd_hop(x);
+      long long d = (long long)hd_dist(x);
       bool keepit;
       if (u == v) {
         keepit = true;  // the self label (v, 0, 0) is never covered
@@ -114,16 +115,18 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
           for (int j0 = 0; j0 < ulen; j0 += 32) {
             int j = j0 + lane;
             if (j < ulen) {
-              uint64_t k1 = keys[ulo + j];
-              int w = (int)lkey_hub(k1);
-              int h1 = (int)lkey_hop(k1);
-              if (w != u && h1 <= h) {
+              int w = (int)hub[ulo + j];
+              if (w != u) {
                 const int32_t* rw = tab_find(T, mask, stride, w);
-                if (rw) {
-                  int32_t t = rw[1 + h - h1];
-                  if (t != kInf32) {
-                    long long c = (long long)lkey_dist(k1) + t;
-                    q = c < q ? c : q;
+                if (rw) {  // hop and distance are read only for hubs v shares
+                  uint32_t x1 = hd[ulo + j];
+                  int h1 = (int)hd_hop(x1);
+                  if (h1 <= h) {
+                    int32_t t = rw[1 + h - h1];
+                    if (t != kInf32) {
+                      long long c = (long long)hd_dist(x1) + t;
+                      q = c < q ? c : q;
+                    }
                   }
                 }
               }
@@ -148,10 +151,10 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
   }
 }
 
-__global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint64_t* __restrict__ keys,
-                          const int32_t* __restrict__ par, const uint8_t* __restrict__ keep,
-                          const int64_t* __restrict__ noff, uint64_t* __restrict__ nkeys,
-                          int32_t* __restrict__ npar) {
+__global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint32_t* __restrict__ hub,
+                          const uint32_t* __restrict__ hd, const int32_t* __restrict__ par,
+                          const uint8_t* __restrict__ keep, const int64_t* __restrict__ noff,
+                          uint32_t* __restrict__ nhub, uint32_t* __restrict__ nhd, int32_t* __restrict__ npar) {
   const int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -163,7 +166,8 @@ __global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint
       unsigned b = __ballot_sync(0xffffffffu, k);
       if (k) {
         int64_t at = dst + __popc(b & ((1u << lane) - 1));
-        nkeys[at] = keys[lo + j];
+        nhub[at] = hub[lo + j];
+        nhd[at] = hd[lo + j];
         npar[at] = par[lo + j];
       }
       dst += __popc(b);
@@ -201,28 +205,33 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_TRY(noff.alloc((int64_t)n + 1));
   HSDL_TRY(next.alloc(1));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
-  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->keys.p, keep.p, kept.p, stride, smem_slots,
-                                             gscratch.p, gslots, next.p);
+  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p, stride,
+                                             smem_slots, gscratch.p, gslots, next.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
   int64_t total = 0;
   HSDL_CUDA(cudaMemcpyAsync(&total, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
-  DevBuf<uint64_t> nkeys;
+  DevBuf<uint32_t> nhub, nhd;
   DevBuf<int32_t> npar;
-  HSDL_TRY(nkeys.alloc(std::max<int64_t>(1, total)));
-  HSDL_TRY(npar.alloc(std::max<int64_t>(1, total)));
-  k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->keys.p, idx->par.p, keep.p, noff.p, nkeys.p, npar.p);
+  HSDL_TRY(nhub.alloc(total + kRowPad));
+  HSDL_TRY(nhd.alloc(total + kRowPad));
+  HSDL_TRY(npar.alloc(total + kRowPad));
+  k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p, keep.p, noff.p, nhub.p,
+                                     nhd.p, npar.p);
   HSDL_LAUNCHED();
   HSDL_CUDA(cudaStreamSynchronize(st));
   std::swap(idx->off.p, noff.p);
   std::swap(idx->off.cap, noff.cap);
-  std::swap(idx->keys.p, nkeys.p);
-  std::swap(idx->keys.cap, nkeys.cap);
+  std::swap(idx->hub.p, nhub.p);
+  std::swap(idx->hub.cap, nhub.cap);
+  std::swap(idx->hd.p, nhd.p);
+  std::swap(idx->hd.cap, nhd.cap);
   std::swap(idx->par.p, npar.p);
   std::swap(idx->par.cap, npar.cap);
   noff.release();
-  nkeys.release();
+  nhub.release();
+  nhd.release();
   npar.release();
   keep.release();
   kept.release();

@@ -393,8 +393,8 @@ __global__ void k_final_len(int32_t n, const int32_t* __restrict__ row_len, int6
 
 __global__ void k_final_copy(int32_t n, const int64_t* __restrict__ row_off, const int32_t* __restrict__ row_len,
                              const uint64_t* __restrict__ keys, const int32_t* __restrict__ par,
-                             const int64_t* __restrict__ foff, uint64_t* __restrict__ fkeys,
-                             int32_t* __restrict__ fpar) {
+                             const int64_t* __restrict__ foff, uint32_t* __restrict__ fhub,
+                             uint32_t* __restrict__ fhd, int32_t* __restrict__ fpar) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -402,13 +402,16 @@ __global__ void k_final_copy(int32_t n, const int64_t* __restrict__ row_off, con
     int64_t src = row_off[v], dst = foff[v];
     int len = row_len[v];
     for (int j = lane; j < len; j += 32) {
-      fkeys[dst + j] = keys[src + j];
+      uint64_t k = keys[src + j];
+      fhub[dst + j] = lkey_hub(k);
+      fhd[dst + j] = lkey_hd(k);
       fpar[dst + j] = par[src + j];
     }
     if (lane == 0) {
       // self label (v, v, 0, 0), pushed by the reference when hub v starts
       // (generation.h:74-85)
-      fkeys[dst + len] = lkey((uint32_t)v, 0, 0);
+      fhub[dst + len] = (uint32_t)v;
+      fhd[dst + len] = hd_pack(0, 0);
       fpar[dst + len] = (int32_t)v;
     }
   }
@@ -636,16 +639,17 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   int64_t total = 0;
   HSDL_CUDA(cudaMemcpyAsync(&total, idx->off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
-  HSDL_TRY(idx->keys.alloc(total));
-  HSDL_TRY(idx->par.alloc(total));
+  HSDL_TRY(idx->hub.alloc(total + kRowPad));
+  HSDL_TRY(idx->hd.alloc(total + kRowPad));
+  HSDL_TRY(idx->par.alloc(total + kRowPad));
   k_final_copy<<<grid * 2, 256, 0, st>>>(n, row_off.p, row_len.p, pool_keys.p, pool_par.p, idx->off.p,
-                                         idx->keys.p, idx->par.p);
+                                         idx->hub.p, idx->hd.p, idx->par.p);
   HSDL_LAUNCHED();
   flen.release();
   release_all();
   int64_t mr = 0;
   HSDL_TRY(row_max(n, idx->off.p, &mr, st));
-  HSDL_TRY(sort_rows(n, idx->off.p, idx->keys.p, idx->par.p, mr, st));
+  HSDL_TRY(sort_rows(n, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p, mr, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
   double t2 = now_s();
   idx->n = n;

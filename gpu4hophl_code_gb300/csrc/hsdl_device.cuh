@@ -8,14 +8,17 @@ namespace hsdl {
 // ---------------------------------------------------------------------------
 // Packed encodings.
 //
-// Label key (the per-vertex label store, 8 B):
-//     hub:28 | hop:4 | distance:32          (bits 63..36 | 35..32 | 31..0)
+// Label key (8 B):
+//     hub:32 | hop:4 | distance:28          (bits 63..32 | 31..28 | 27..0)
 // Unsigned order of the key is exactly the reference's label order
 // (hub asc, hop asc, distance asc; compare_hop_constrained_two_hop_label,
 // CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:373-387),
-// so sorting keys sorts labels.  parent_vertex is kept in a parallel int32
-// array.  Limits: vertex ids < 2^28 (the reference itself stops at 10^7,
-// generation.h:528-532), hop <= 14, distance < 2^31.
+// so sorting keys sorts labels.  A resident index stores the two halves as
+// separate arrays (hub[], hd[] = hop:4|distance:28) so that joins can stream
+// 4-byte hub ids and fetch hop and distance only on a hub match;
+// parent_vertex is kept in a parallel int32 array.  Limits: vertex ids < 2^28
+// (the reference itself stops at 10^7, generation.h:528-532), hop <= 14,
+// distance < 2^28 (K * max edge weight < 2^28).
 //
 // Candidate key (per-slot search state, 8 B):
 //     distance:32 | hop:4 | parent:28
@@ -29,12 +32,19 @@ constexpr int32_t kMaxK = 14;
 constexpr int32_t kInf32 = 0x7F7F7F7F;  // "no value" in hub tables (memset 0x7F)
 constexpr int32_t kEmptyKey = 0x7F7F7F7F;
 
+constexpr uint32_t kDistMask = (1u << 28) - 1;
+
+__host__ __device__ inline uint32_t hd_pack(uint32_t hop, uint32_t dist) { return (hop << 28) | dist; }
+__host__ __device__ inline uint32_t hd_hop(uint32_t x) { return x >> 28; }
+__host__ __device__ inline uint32_t hd_dist(uint32_t x) { return x & kDistMask; }
+
 __host__ __device__ inline uint64_t lkey(uint32_t hub, uint32_t hop, uint32_t dist) {
-  return ((uint64_t)hub << 36) | ((uint64_t)hop << 32) | (uint64_t)dist;
+  return ((uint64_t)hub << 32) | (uint64_t)hd_pack(hop, dist);
 }
-__host__ __device__ inline uint32_t lkey_hub(uint64_t k) { return (uint32_t)(k >> 36); }
-__host__ __device__ inline uint32_t lkey_hop(uint64_t k) { return (uint32_t)(k >> 32) & 15u; }
-__host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return (uint32_t)k; }
+__host__ __device__ inline uint32_t lkey_hub(uint64_t k) { return (uint32_t)(k >> 32); }
+__host__ __device__ inline uint32_t lkey_hd(uint64_t k) { return (uint32_t)k; }
+__host__ __device__ inline uint32_t lkey_hop(uint64_t k) { return hd_hop((uint32_t)k); }
+__host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return hd_dist((uint32_t)k); }
 
 __host__ __device__ inline uint64_t ckey(uint32_t dist, uint32_t hop, uint32_t parent) {
   return ((uint64_t)dist << 32) | ((uint64_t)hop << 28) | (uint64_t)parent;

@@ -90,13 +90,18 @@ struct hsdl_graph_impl {
   std::vector<int64_t> h_rp;  // host copy of row_ptr (for sizing decisions)
 };
 
-// A built (or imported) label index resident in HBM.  Rows are sorted by the
-// packed label key; parents travel in a parallel array.
+// A built (or imported) label index resident in HBM, per-vertex CSR in three
+// parallel arrays: hub[] (hub_vertex), hd[] (hop:4 | distance:28) and par[]
+// (parent_vertex).  Rows are sorted by (hub, hd), the reference's order.
+// The arrays carry kRowPad spare entries at the end so that 16-byte aligned
+// bulk copies of any row stay inside the allocation.
+constexpr int64_t kRowPad = 8;
 struct hsdl_index_impl {
   int32_t n = 0, K = 0;
   bool cleaned = false;
   DevBuf<int64_t> off;    // n+1
-  DevBuf<uint64_t> keys;  // label keys (hub:28 | hop:4 | dist:32)
+  DevBuf<uint32_t> hub;   // hub_vertex
+  DevBuf<uint32_t> hd;    // hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
@@ -114,7 +119,8 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 int clean_index(hsdl_index_impl* idx);
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st);
-int sort_rows(int32_t n, const int64_t* d_off, uint64_t* keys, int32_t* par, int64_t max_row, cudaStream_t st);
+int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int32_t* par, int64_t max_row,
+              cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total
 
 }  // namespace hsdl

@@ -8,11 +8,12 @@
 // three launches and a synchronisation per query.
 //
 // Here one warp answers one query and a launch answers the whole batch.  The
-// lanes take 32 consecutive labels of the shorter row at a time; each lane
-// finds its hub in the longer row by binary search on the packed keys (rows
-// are sorted by key = (hub, hop, distance)), scans that hub's run, and the
-// warp reduces with a min.  The search window of the next 32 labels starts
-// where the last lane's search ended.
+// shorter row A is cut into 32 contiguous pieces, one per lane; each lane
+// finds where its piece's first hub falls in the longer row B (one binary
+// search) and then merges its piece against B with two pointers, streaming
+// the 4-byte hub ids of both rows and reading hop and distance only on a hub
+// match.  A hub's run in B is scanned with the reference's hop-sum break, and
+// the warp reduces the lanes' minima.
 #include <algorithm>
 #include <climits>
 
@@ -25,10 +26,10 @@ namespace {
 
 constexpr int kQueryThreads = 256;
 
-__device__ inline int64_t lower_bound_key(const uint64_t* __restrict__ a, int64_t lo, int64_t hi, uint64_t key) {
+__device__ inline int64_t lower_bound_hub(const uint32_t* __restrict__ a, int64_t lo, int64_t hi, uint32_t w) {
   while (lo < hi) {
     int64_t mid = (lo + hi) >> 1;
-    if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
+    if (__ldg(a + mid) < w) lo = mid + 1; else hi = mid;
   }
   return lo;
 }
@@ -37,7 +38,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(int32_t n, int64_t nq, 
                                                          const int32_t* __restrict__ qt,
                                                          const int32_t* __restrict__ qk,
                                                          const int64_t* __restrict__ off,
-                                                         const uint64_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ hub,
+                                                         const uint32_t* __restrict__ hd,
                                                          int32_t* __restrict__ out) {
   const int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -55,36 +57,31 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(int32_t n, int64_t nq, 
       best = INT_MAX;
     } else {
       int64_t a0 = off[s], a1 = off[s + 1], b0 = off[t], b1 = off[t + 1];
-      if (a1 - a0 > b1 - b0) {  // probe with the shorter row
+      if (a1 - a0 > b1 - b0) {  // A = the shorter row
         int64_t x = a0; a0 = b0; b0 = x;
         x = a1; a1 = b1; b1 = x;
       }
-      int64_t window = b0;
-      for (int64_t j0 = a0; j0 < a1; j0 += 32) {
-        int64_t j = j0 + lane;
-        int64_t pos = window;
-        if (j < a1) {
-          uint64_t ka = __ldg(keys + j);
-          int h1 = (int)lkey_hop(ka);
-          uint32_t w = lkey_hub(ka);
-          pos = lower_bound_key(keys, window, b1, lkey(w, 0, 0));
-          if (h1 <= k) {
-            for (int64_t p = pos; p < b1; p++) {
-              uint64_t kb = __ldg(keys + p);
-              if (lkey_hub(kb) != w) break;
-              if (h1 + (int)lkey_hop(kb) > k) break;  // rows are hop-sorted within a hub
-              long long c = (long long)lkey_dist(ka) + lkey_dist(kb);
-              best = c < best ? c : best;
-            }
+      const int64_t la = a1 - a0;
+      const int64_t pa = a0 + (la * lane) / 32, pe = a0 + (la * (lane + 1)) / 32;
+      if (pa < pe) {
+        int64_t pb = lower_bound_hub(hub, b0, b1, __ldg(hub + pa));
+        for (int64_t i = pa; i < pe && pb < b1; i++) {
+          const uint32_t w = __ldg(hub + i);
+          uint32_t hb = __ldg(hub + pb);
+          while (hb < w && ++pb < b1) hb = __ldg(hub + pb);
+          if (pb >= b1) break;
+          if (hb != w) continue;
+          const uint32_t xa = __ldg(hd + i);
+          const int h1 = (int)hd_hop(xa);
+          if (h1 > k) continue;
+          const long long d1 = hd_dist(xa);
+          for (int64_t p = pb; p < b1 && __ldg(hub + p) == w; p++) {
+            const uint32_t xb = __ldg(hd + p);
+            if (h1 + (int)hd_hop(xb) > k) break;  // rows are hop-sorted within a hub
+            const long long c = d1 + hd_dist(xb);
+            best = c < best ? c : best;
           }
         }
-        // next chunk's hubs are larger: search from the largest position found
-        int64_t mx = pos;
-        for (int o = 16; o > 0; o >>= 1) {
-          int64_t y = __shfl_xor_sync(0xffffffffu, mx, o);
-          mx = y > mx ? y : mx;
-        }
-        window = mx;
       }
       best = warp_min_ll(best);
     }
@@ -102,7 +99,7 @@ int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
   int64_t blocks = (warps_needed * 32 + kQueryThreads - 1) / kQueryThreads;
   int64_t max_blocks = (int64_t)sms * 16;
   k_query<<<(unsigned)std::min(blocks, max_blocks), kQueryThreads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p,
-                                                                             idx->keys.p, out);
+                                                                             idx->hub.p, idx->hd.p, out);
   HSDL_LAUNCHED();
   return HSDL_OK;
 }

@@ -13,7 +13,7 @@
  * file:line inside the reference project (rucdatascience/GPU4HopHL_code).
  *
  * Limits (checked, HSDL_ERR_INVALID when exceeded): vertex count < 2^28,
- * hop bound 1 <= K <= 14, edge weights >= 1 and K * max weight < 2^31.
+ * hop bound 1 <= K <= 14, edge weights >= 1 and K * max weight < 2^28.
  */
 #ifndef HSDL_H
 #define HSDL_H
