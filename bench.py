@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--K", type=int, default=5)
     ap.add_argument("--cpu-baseline-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-rates", default="5e6,2e7,5e7,1e8,2e8,0",
+                    help="offered Poisson rates (q/s) for the serving loop; 0 = as fast as the ring allows")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -230,9 +234,30 @@ def run_ours(args, dist, rank, world, local):
     for _ in range(args.steps):
         _native.check(L.hsdl_query_batch(idx.handle, args.queries, P(hs), P(ht), P(hk), P(ho)))
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    clk = clocks.stop()
-    e2e = world * args.queries * args.steps / e2e_s
+    e2e_batch = world * args.queries * args.steps / e2e_s
     assert np.array_equal(ho.numpy(), answers), "e2e answers differ from the device-path answers"
+
+    # persistent serving loop: open-loop Poisson arrivals from host memory
+    serving = None
+    if not args.no_serve:
+        srv = H.Server()
+        gid = srv.add_index(idx)
+        runs = []
+        for rate in [float(x) for x in args.serve_rates.split(",")]:
+            nreq = args.queries if rate <= 0 else int(min(args.queries, max(100000, rate * args.serve_seconds)))
+            barrier(dist)
+            r = srv.loadgen(np.full(nreq, gid, np.int32), s[:nreq], t[:nreq], k[:nreq], offered_qps=rate)
+            assert np.array_equal(r["answers"], answers[:nreq]), "serving answers differ from the batched path"
+            runs.append({"offered_qps": rate, "requests": nreq, "qps": round(r["achieved_qps"], 1),
+                         "p50_us": round(r["p50_us"], 1), "p99_us": round(r["p99_us"], 1),
+                         "p999_us": round(r["p999_us"], 1), "max_us": round(r["max_us"], 1)})
+        srv.close()
+        ok = [x for x in runs if x["p99_us"] < 1000.0]
+        best = max(ok, key=lambda x: x["qps"]) if ok else max(runs, key=lambda x: x["qps"])
+        serving = {"qps": best["qps"], "p50_us": best["p50_us"], "p99_us": best["p99_us"],
+                   "p999_us": best["p999_us"], "offered_qps": best["offered_qps"],
+                   "p99_under_1ms": bool(ok), "runs": runs}
+    clk = clocks.stop()
 
     # roofline of the query kernel
     peaks = {}
@@ -271,8 +296,16 @@ def run_ours(args, dist, rank, world, local):
                        "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (label index "
                              f"{info['device_bytes'] / 1e9:.1f} GB)"},
-            "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": 12 * args.queries,
-                    "d2h_bytes_per_step": 4 * args.queries},
+            "e2e": ({"value": serving["qps"], "unit": "queries/s", "path": "persistent serving loop "
+                     "(hsdl_serve_*): requests read from pinned host memory, answers written to pinned host memory",
+                     "h2d_bytes_per_step": 16 * args.queries, "d2h_bytes_per_step": 8 * args.queries,
+                     "p50_us": serving["p50_us"], "p99_us": serving["p99_us"], "offered_qps": serving["offered_qps"]}
+                    if serving else
+                    {"value": round(e2e_batch, 1), "unit": "queries/s", "path": "hsdl_query_batch",
+                     "h2d_bytes_per_step": 12 * args.queries, "d2h_bytes_per_step": 4 * args.queries}),
+            "e2e_batch": {"value": round(e2e_batch, 1), "unit": "queries/s", "path": "hsdl_query_batch, pinned buffers",
+                          "h2d_bytes_per_step": 12 * args.queries, "d2h_bytes_per_step": 4 * args.queries},
+            "serving": serving,
             "build": {"seconds": round(build_s, 3), "generate_s": round(info["time_generate_s"], 3),
                       "sort_s": round(info["time_sort_s"], 3), "clean_s": round(info["time_clean_s"], 3),
                       "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],

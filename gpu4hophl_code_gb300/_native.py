@@ -48,6 +48,29 @@ class hsdl_index_info(C.Structure):
                 ("time_clean_s", C.c_double), ("max_row", C.c_int64)]
 
 
+class hsdl_serve_opts(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("ctas", C.c_int32), ("ring_log2", C.c_int32),
+                ("max_indexes", C.c_int32), ("budget_bytes", C.c_int64), ("idle_exit_s", C.c_double)]
+
+
+class hsdl_loadgen_opts(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("reserved", C.c_int32), ("n", C.c_int64), ("g", C.c_void_p),
+                ("s", C.c_void_p), ("t", C.c_void_p), ("k", C.c_void_p), ("answers", C.c_void_p),
+                ("offered_qps", C.c_double), ("seed", C.c_uint64)]
+
+
+class hsdl_loadgen_result(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("seconds", C.c_double), ("achieved_qps", C.c_double),
+                ("offered_qps", C.c_double), ("p50_us", C.c_double), ("p90_us", C.c_double),
+                ("p99_us", C.c_double), ("p999_us", C.c_double), ("max_us", C.c_double)]
+
+
+class hsdl_serve_counters(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("processed", C.c_int64), ("bad_requests", C.c_int64),
+                ("resident_graphs", C.c_int64), ("pending_builds", C.c_int64), ("resident_bytes", C.c_int64),
+                ("builds_done", C.c_int64), ("loop_running", C.c_int32), ("reserved", C.c_int32)]
+
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -82,6 +105,18 @@ SIGNATURES = {
     "hsdl_save_labels": (C.c_int, [P, C.c_char_p]),
     "hsdl_load_labels": (C.c_int, [C.c_char_p, I32, PP]),
     "hsdl_index_destroy": (C.c_int, [P]),
+    "hsdl_serve_opts_default": (None, [C.POINTER(hsdl_serve_opts)]),
+    "hsdl_serve_create": (C.c_int, [C.POINTER(hsdl_serve_opts), PP]),
+    "hsdl_serve_add_index": (C.c_int, [P, P, C.POINTER(I32)]),
+    "hsdl_serve_submit_build": (C.c_int, [P, P, I32, C.POINTER(I32)]),
+    "hsdl_serve_graph_state": (C.c_int, [P, I32, C.POINTER(I32), C.POINTER(I64)]),
+    "hsdl_serve_wait_graph": (C.c_int, [P, I32, C.c_double]),
+    "hsdl_serve_remove_graph": (C.c_int, [P, I32]),
+    "hsdl_serve_submit": (C.c_int, [P, I64, P, P, P, P, C.POINTER(I64)]),
+    "hsdl_serve_wait": (C.c_int, [P, I64, I64, P, C.c_double]),
+    "hsdl_serve_loadgen": (C.c_int, [P, C.POINTER(hsdl_loadgen_opts), C.POINTER(hsdl_loadgen_result)]),
+    "hsdl_serve_stats": (C.c_int, [P, C.POINTER(hsdl_serve_counters)]),
+    "hsdl_serve_destroy": (C.c_int, [P]),
 }
 
 _lib = None

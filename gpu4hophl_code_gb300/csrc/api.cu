@@ -76,6 +76,15 @@ int new_index(hsdl_index** out) {
     set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     return HSDL_ERR_CUDA;
   }
+  // the query kernels' error word, allocated here so that no query call allocates
+  int rc = idx->qerr.alloc(1);
+  if (rc == HSDL_OK && cudaMemset(idx->qerr.p, 0, sizeof(unsigned int)) != cudaSuccess) rc = HSDL_ERR_CUDA;
+  if (rc != HSDL_OK) {
+    cudaStreamDestroy(idx->stream);
+    delete idx;
+    set_error("query error word allocation failed");
+    return rc;
+  }
   *out = idx;
   return HSDL_OK;
 }
@@ -87,6 +96,7 @@ void free_index(hsdl_index* idx) {
   idx->hub.release();
   idx->hd.release();
   idx->par.release();
+  idx->qerr.release();
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;
 }
@@ -420,6 +430,7 @@ int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_
   }
   HSDL_CUDA(cudaFreeAsync(d, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
+  if (rc == HSDL_OK) rc = query_error(idx);
   return rc;
 }
 

@@ -103,6 +103,7 @@ struct hsdl_index_impl {
   DevBuf<uint32_t> hub;   // hub_vertex
   DevBuf<uint32_t> hd;    // hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
+  DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;
@@ -119,6 +120,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 int clean_index(hsdl_index_impl* idx);
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st);
+int query_error(hsdl_index_impl* idx);  // HSDL_ERR_TIMEOUT (and clears) if a query kernel flagged one
 int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int32_t* par, int64_t max_row,
               cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total

@@ -1,0 +1,107 @@
+// The (s, t, k) distance join on a resident label index, one warp per query.
+//
+// Reference: hop_constrained_extract_distance
+// (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:144-222): the
+// minimum d1 + d2 over label pairs of a common hub with h1 + h2 <= k;
+// INT_MAX for k < 0, then 0 for s == t, then INT_MAX for k == 0, and INT_MAX
+// when no pair qualifies.
+//
+// The merged hub order of the two rows is cut into 32 equal pieces (merge
+// path: each lane finds its split with one binary search along its diagonal,
+// A's labels ordered before B's on equal hubs), and every lane merges its
+// piece with two pointers, streaming 4-byte hub ids and reading hop and
+// distance only on a hub match.  When the lane takes a label of A with hub w,
+// B's run of hub w starts at the lane's B pointer; it is scanned with the
+// reference's hop-sum break (possibly past the lane's piece).  A warp min
+// combines the lanes.
+#pragma once
+#include <climits>
+
+#include "hsdl_device.cuh"
+
+namespace hsdl {
+
+// One lane's share of the merge-path join of hub rows A (la labels) and B (lb
+// labels) under hop bound k >= 1; returns the lane's minimum (INT_MAX if none).
+// A and B may point to shared or global memory; Ahd/Bhd are the matching
+// hop|distance words in global memory (read only on hub matches).
+__device__ inline long long lane_merge(const uint32_t* A, int la, const uint32_t* B, int lb,
+                                       const uint32_t* __restrict__ Ahd, const uint32_t* __restrict__ Bhd, int k) {
+  const int lane = lane_id();
+  long long best = INT_MAX;
+  const int tot = la + lb;
+  const int d0 = (int)(((int64_t)tot * lane) >> 5), d1 = (int)(((int64_t)tot * (lane + 1)) >> 5);
+  if (d0 < d1) {
+    // merge-path split of diagonal d0: ia labels of A precede it
+    int lo = max(0, d0 - lb), hi = min(d0, la);
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (A[mid] <= B[d0 - 1 - mid]) lo = mid + 1; else hi = mid;
+    }
+    int ia = lo, ib = d0 - lo;
+    uint32_t wa = ia < la ? A[ia] : 0xFFFFFFFFu;
+    uint32_t wb = ib < lb ? B[ib] : 0xFFFFFFFFu;
+    for (int step = d0; step < d1; step++) {
+      if (ia < la && (ib >= lb || wa <= wb)) {
+        if (wa == wb) {
+          const uint32_t xa = __ldg(Ahd + ia);
+          const int h1 = (int)hd_hop(xa);
+          if (h1 <= k) {
+            const long long da = hd_dist(xa);
+            for (int p = ib; p < lb && B[p] == wa; p++) {
+              const uint32_t xb = __ldg(Bhd + p);
+              if (h1 + (int)hd_hop(xb) > k) break;  // rows are hop-sorted within a hub
+              const long long c = da + hd_dist(xb);
+              best = c < best ? c : best;
+            }
+          }
+        }
+        ia++;
+        wa = ia < la ? A[ia] : 0xFFFFFFFFu;
+      } else {
+        ib++;
+        wb = ib < lb ? B[ib] : 0xFFFFFFFFu;
+      }
+    }
+  }
+  return best;
+}
+
+// Checks that decide an answer without a join; returns true and sets *ans.
+__device__ inline bool trivial_answer(int32_t n, int s, int t, int k, int32_t* ans) {
+  if (s < 0 || s >= n || t < 0 || t >= n) {
+    *ans = INT_MAX;  // ids outside the index answer "unreachable"
+    return true;
+  }
+  if (k < 0) {
+    *ans = INT_MAX;
+    return true;
+  }
+  if (s == t) {
+    *ans = 0;
+    return true;
+  }
+  if (k == 0) {
+    *ans = INT_MAX;
+    return true;
+  }
+  return false;
+}
+
+__device__ inline int32_t clamp_answer(long long best) { return best >= INT_MAX ? INT_MAX : (int32_t)best; }
+
+// The whole answer of (s, t, k) with both rows read from global memory.
+__device__ inline int32_t warp_query(int32_t n, const int64_t* __restrict__ off, const uint32_t* __restrict__ hub,
+                                     const uint32_t* __restrict__ hd, const int s, const int t, const int k) {
+  int32_t ans;
+  if (trivial_answer(n, s, t, k, &ans)) return ans;
+  int64_t a0 = off[s], a1 = off[s + 1], b0 = off[t], b1 = off[t + 1];
+  if (a1 - a0 > b1 - b0) {  // A = the shorter row
+    int64_t x = a0; a0 = b0; b0 = x;
+    x = a1; a1 = b1; b1 = x;
+  }
+  long long best = lane_merge(hub + a0, (int)(a1 - a0), hub + b0, (int)(b1 - b0), hd + a0, hd + b0, k);
+  return clamp_answer(warp_min_ll(best));
+}
+
+}  // namespace hsdl

@@ -1,0 +1,742 @@
+// Persistent, device-resident serving loop for (graph, s, t, k) queries over
+// many resident label indexes, with index builds admitted concurrently.
+//
+// The reference answers queries one at a time on the host
+// (hop_constrained_extract_distance, CPU_HopHL/include/HBPLL/
+// hop_constrained_two_hop_labels.h:144) or with three launches and a sync per
+// query (gpu_query, Query_mdnd/src/gpu_query.cu:84-178); it has no serving
+// mode.  Here one kernel stays resident:
+//
+//  * Requests {graph, s, t, k} go into a ring in pinned host memory that the
+//    GPU reads directly (mapped, coherent over NVLink-C2C on Grace systems).
+//    The host publishes them by advancing `tail` with a release store.
+//  * Every warp of the persistent kernel claims up to 32 published tickets at
+//    a time with a CAS on the device-side `head` (continuous batching: a warp
+//    takes whatever has arrived, across all resident graphs, as soon as it is
+//    free), answers them one by one with the merge-path join
+//    (query_join.cuh), and writes each answer with its ticket into a
+//    completion ring in pinned host memory as one 8-byte store.
+//  * Idle warps poll with __nanosleep.  Every wait is bounded: after
+//    `idle_exit_s` without work, or when the host sets `stop`, the kernel
+//    returns; the host relaunches it on the next submission.
+//  * Resident indexes are described in a device table; builds requested
+//    through the server run on a worker thread on their own stream while the
+//    loop keeps serving, admitted when resident + pending estimated label
+//    bytes fit the budget.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "hsdl_device.cuh"
+#include "hsdl_runtime.h"
+#include "query_join.cuh"
+
+namespace hsdl {
+
+namespace {
+
+struct IndexDesc {
+  const int64_t* off;
+  const uint32_t* hub;
+  const uint32_t* hd;
+  int32_t n;
+  int32_t valid;
+};
+
+struct ServeReq {
+  int32_t g, s, t, k;
+};
+
+struct DevCtl {
+  unsigned long long head;       // next ticket to claim
+  unsigned long long processed;  // tickets answered
+  unsigned long long bad;        // requests naming no resident graph
+  unsigned int exit_reason;      // 1 idle, 2 stop
+  unsigned int pad;
+};
+
+struct HostCtl {
+  unsigned long long tail;  // tickets published by the host
+  unsigned int stop;        // 1: return as soon as the claimed work is done
+  unsigned int pad;
+};
+
+__device__ inline unsigned long long ld_acquire_sys(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline unsigned int ld_volatile_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline int4 ld_volatile_v4(const int4* p) {
+  int4 v;
+  asm volatile("ld.volatile.global.v4.s32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p)
+               : "memory");
+  return v;
+}
+__device__ inline void st_relaxed_sys(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ inline long long globaltimer_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
+                                               unsigned long long* comp, unsigned long long mask,
+                                               const IndexDesc* descs, int32_t max_idx, long long idle_ns) {
+  const int lane = lane_id();
+  long long idle_start = globaltimer_ns();
+  for (;;) {
+    unsigned long long tail = 0, h = 0;
+    int ok = 0, cnt = 0;
+    if (lane == 0) {
+      tail = ld_acquire_sys(&hctl->tail);
+      h = *(volatile unsigned long long*)&ctl->head;
+      if (h < tail) {
+        cnt = (int)min((unsigned long long)32, tail - h);
+        ok = atomicCAS(&ctl->head, h, h + cnt) == h;
+      }
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok) {
+      h = __shfl_sync(0xffffffffu, h, 0);
+      cnt = __shfl_sync(0xffffffffu, cnt, 0);
+      int4 r = make_int4(-1, 0, 0, 0);
+      if (lane < cnt) r = ld_volatile_v4(ring + ((h + lane) & mask));
+      int32_t mine = INT_MAX;
+      for (int j = 0; j < cnt; j++) {
+        const int g = __shfl_sync(0xffffffffu, r.x, j);
+        const int s = __shfl_sync(0xffffffffu, r.y, j);
+        const int t = __shfl_sync(0xffffffffu, r.z, j);
+        const int k = __shfl_sync(0xffffffffu, r.w, j);
+        int32_t ans = INT_MAX;
+        bool valid = g >= 0 && g < max_idx;
+        IndexDesc d;
+        if (valid) {
+          d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[g].off);
+          d.hub = (const uint32_t*)__ldcg((const unsigned long long*)&descs[g].hub);
+          d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[g].hd);
+          d.n = __ldcg(&descs[g].n);
+          d.valid = __ldcg(&descs[g].valid);
+          valid = d.valid != 0;
+        }
+        if (valid) ans = warp_query(d.n, d.off, d.hub, d.hd, s, t, k);
+        else if (lane == 0) atomicAdd(&ctl->bad, 1ull);
+        if (lane == j) mine = ans;
+      }
+      if (lane < cnt) {
+        unsigned long long tk = h + lane;
+        st_relaxed_sys(comp + (tk & mask), ((unsigned long long)(uint32_t)(tk + 1) << 32) | (uint32_t)mine);
+      }
+      __threadfence_system();
+      if (lane == 0) atomicAdd(&ctl->processed, (unsigned long long)cnt);
+      idle_start = globaltimer_ns();
+      continue;
+    }
+    // nothing claimed: stop, idle exit or back off
+    unsigned int stop = 0;
+    if (lane == 0) stop = ld_volatile_u32(&hctl->stop);
+    stop = __shfl_sync(0xffffffffu, stop, 0);
+    if (stop) {
+      if (lane == 0) atomicMax(&ctl->exit_reason, 2u);
+      return;
+    }
+    tail = __shfl_sync(0xffffffffu, tail, 0);
+    h = __shfl_sync(0xffffffffu, h, 0);
+    if (h >= tail) {
+      if (globaltimer_ns() - idle_start > idle_ns) {
+        if (lane == 0) atomicMax(&ctl->exit_reason, 1u);
+        return;
+      }
+      __nanosleep(200);
+    }
+  }
+}
+
+double mono_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+int64_t mono_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+}  // namespace
+
+struct ServerImpl {
+  hsdl_serve_opts opts;
+  int sms = 1;
+  cudaStream_t stream = nullptr;   // the persistent kernel
+  cudaStream_t side = nullptr;     // descriptor updates
+  DevBuf<DevCtl> ctl;
+  DevBuf<IndexDesc> descs;
+  HostCtl* hctl = nullptr;         // pinned, mapped
+  HostCtl* hctl_dev = nullptr;
+  int4* ring = nullptr;            // pinned, mapped
+  int4* ring_dev = nullptr;
+  unsigned long long* comp = nullptr;  // pinned, mapped
+  unsigned long long* comp_dev = nullptr;
+  uint64_t cap = 0, mask = 0;
+  uint64_t tail = 0;      // host copy of published tickets
+  uint64_t consumed = 0;  // tickets whose answers the host has read
+  bool running = false;
+  std::mutex mu;          // submission / consumption / launch state
+  // resident indexes
+  struct Slot {
+    hsdl_index* idx = nullptr;
+    bool owned = false;
+    int state = 0;  // 0 free, 1 pending build, 2 resident, 3 failed
+    int64_t est_bytes = 0, bytes = 0;
+    std::string error;
+  };
+  std::vector<Slot> slots;
+  std::mutex slot_mu;
+  std::condition_variable slot_cv;
+  // build worker
+  struct BuildJob {
+    int32_t gid;
+    hsdl_graph* g;
+    int32_t K;
+  };
+  std::deque<BuildJob> jobs;
+  std::thread worker;
+  bool quit = false;
+  int64_t builds_done = 0;
+};
+
+namespace {
+
+int launch_if_needed(ServerImpl* S) {
+  if (S->running) {
+    cudaError_t q = cudaStreamQuery(S->stream);
+    if (q == cudaErrorNotReady) return HSDL_OK;
+    if (q != cudaSuccess) {
+      set_error(std::string("serving kernel: ") + cudaGetErrorString(q));
+      return HSDL_ERR_CUDA;
+    }
+    S->running = false;  // it returned (idle)
+  }
+  HSDL_CUDA(cudaMemsetAsync(&S->ctl.p->exit_reason, 0, sizeof(unsigned int), S->stream));
+  long long idle_ns = (long long)(S->opts.idle_exit_s * 1e9);
+  k_serve<<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
+                                               S->descs.p, S->opts.max_indexes, idle_ns);
+  HSDL_LAUNCHED();
+  S->running = true;
+  return HSDL_OK;
+}
+
+int write_desc(ServerImpl* S, int32_t gid, hsdl_index* idx, bool valid) {
+  IndexDesc d{};
+  if (idx) {
+    d.off = idx->off.p;
+    d.hub = idx->hub.p;
+    d.hd = idx->hd.p;
+    d.n = idx->n;
+  }
+  d.valid = valid ? 1 : 0;
+  HSDL_CUDA(cudaMemcpyAsync(S->descs.p + gid, &d, sizeof(d), cudaMemcpyHostToDevice, S->side));
+  HSDL_CUDA(cudaStreamSynchronize(S->side));
+  return HSDL_OK;
+}
+
+// Label bytes of an index of n vertices and m edges at hop bound K, for
+// admission only: labels per vertex ~ 0.53 sqrt(n) (avg_deg/10) (K/5), capped
+// by n (K+1), fitted on Chung-Lu graphs of 3*10^4 .. 10^6 vertices at K = 5;
+// 12 bytes per label resident.  Replaced by the measured size once built.
+int64_t estimate_label_bytes(int32_t n, int64_t m2, int32_t K) {
+  double avg_deg = n ? (double)m2 / n : 0.0;
+  double per_v = 0.53 * std::sqrt((double)n) * std::max(0.25, avg_deg / 10.0) * ((double)K / 5.0);
+  per_v = std::min(per_v, (double)n * (K + 1));
+  per_v = std::max(per_v, 1.0);
+  return (int64_t)(12.0 * per_v * n) + 8 * ((int64_t)n + 1);
+}
+
+int64_t resident_bytes_locked(ServerImpl* S) {
+  int64_t b = 0;
+  for (auto& s : S->slots) {
+    if (s.state == 1) b += s.est_bytes;
+    if (s.state == 2) b += s.bytes;
+  }
+  return b;
+}
+
+void worker_main(ServerImpl* S) {
+  for (;;) {
+    ServerImpl::BuildJob job;
+    {
+      std::unique_lock<std::mutex> lk(S->slot_mu);
+      S->slot_cv.wait(lk, [&] { return S->quit || !S->jobs.empty(); });
+      if (S->quit) return;
+      job = S->jobs.front();
+      S->jobs.pop_front();
+    }
+    hsdl_build_opts o;
+    hsdl_build_opts_default(&o);
+    hsdl_index* idx = nullptr;
+    int rc = hsdl_build(job.g, job.K, &o, &idx);
+    std::string err = rc == HSDL_OK ? "" : hsdl_last_error();
+    if (rc == HSDL_OK) rc = write_desc(S, job.gid, idx, true);
+    {
+      std::lock_guard<std::mutex> lk(S->slot_mu);
+      auto& sl = S->slots[job.gid];
+      if (rc == HSDL_OK) {
+        hsdl_index_info info;
+        hsdl_index_get_info(idx, &info);
+        sl.idx = idx;
+        sl.owned = true;
+        sl.bytes = info.device_bytes;
+        sl.state = 2;
+      } else {
+        if (idx) hsdl_index_destroy(idx);
+        sl.state = 3;
+        sl.error = err;
+      }
+      S->builds_done++;
+    }
+    S->slot_cv.notify_all();
+  }
+}
+
+int alloc_slot_locked(ServerImpl* S, int32_t* gid) {
+  for (size_t i = 0; i < S->slots.size(); i++) {
+    if (S->slots[i].state == 0) {
+      *gid = (int32_t)i;
+      return HSDL_OK;
+    }
+  }
+  set_error("no free graph slot (max_indexes reached)");
+  return HSDL_ERR_FULL;
+}
+
+// Waits until every published ticket has been answered (used before an index
+// is retired so no in-flight query reads it).
+int drain(ServerImpl* S, double timeout_s) {
+  double t0 = mono_s();
+  for (;;) {
+    unsigned long long processed = 0;
+    HSDL_CUDA(cudaMemcpyAsync(&processed, &S->ctl.p->processed, sizeof(processed), cudaMemcpyDeviceToHost, S->side));
+    HSDL_CUDA(cudaStreamSynchronize(S->side));
+    if (processed >= S->tail) return HSDL_OK;
+    if (mono_s() - t0 > timeout_s) {
+      set_error("serving loop did not drain within the timeout");
+      return HSDL_ERR_TIMEOUT;
+    }
+    HSDL_TRY(launch_if_needed(S));
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+}  // namespace
+
+}  // namespace hsdl
+
+using namespace hsdl;
+
+struct hsdl_server : hsdl::ServerImpl {};
+
+#define SRV_ARG(cond, msg)     \
+  do {                         \
+    if (!(cond)) {             \
+      set_error(msg);          \
+      return HSDL_ERR_INVALID; \
+    }                          \
+  } while (0)
+
+extern "C" {
+
+void hsdl_serve_opts_default(hsdl_serve_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->struct_size = (int32_t)sizeof(hsdl_serve_opts);
+  o->ctas = 0;
+  o->ring_log2 = 22;
+  o->max_indexes = 1024;
+  o->budget_bytes = (int64_t)120 << 30;
+  o->idle_exit_s = 0.5;
+}
+
+int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
+  SRV_ARG(out, "null output");
+  hsdl_serve_opts o;
+  hsdl_serve_opts_default(&o);
+  if (opts) {
+    SRV_ARG(opts->struct_size == (int32_t)sizeof(hsdl_serve_opts), "hsdl_serve_opts.struct_size mismatch");
+    o = *opts;
+  }
+  SRV_ARG(o.ring_log2 >= 10 && o.ring_log2 <= 26, "ring_log2 must be in [10, 26]");
+  SRV_ARG(o.max_indexes >= 1 && o.max_indexes <= (1 << 20), "max_indexes out of range");
+  SRV_ARG(o.idle_exit_s > 0 && o.idle_exit_s <= 60, "idle_exit_s must be in (0, 60]");
+  auto* S = new hsdl_server();
+  S->opts = o;
+  S->sms = device_sm_count();
+  if (S->opts.ctas <= 0) S->opts.ctas = S->sms * 2;
+  S->cap = 1ull << o.ring_log2;
+  S->mask = S->cap - 1;
+  auto fail = [&](int rc) {
+    hsdl_serve_destroy(S);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    return fail(HSDL_ERR_CUDA);
+  }
+  int rc = S->ctl.alloc(1);
+  if (rc == HSDL_OK) rc = S->descs.alloc(o.max_indexes);
+  if (rc != HSDL_OK) return fail(rc);
+  cudaError_t e = cudaHostAlloc((void**)&S->hctl, sizeof(HostCtl), cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e == cudaSuccess)
+    e = cudaHostAlloc((void**)&S->ring, sizeof(int4) * S->cap, cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e == cudaSuccess)
+    e = cudaHostAlloc((void**)&S->comp, sizeof(unsigned long long) * S->cap,
+                      cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&S->hctl_dev, S->hctl, 0);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&S->ring_dev, S->ring, 0);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&S->comp_dev, S->comp, 0);
+  if (e != cudaSuccess) {
+    set_error(std::string("pinned ring allocation: ") + cudaGetErrorString(e));
+    return fail(HSDL_ERR_NOMEM);
+  }
+  std::memset(S->hctl, 0, sizeof(HostCtl));
+  std::memset(S->comp, 0, sizeof(unsigned long long) * S->cap);
+  if (cudaMemset(S->ctl.p, 0, sizeof(DevCtl)) != cudaSuccess ||
+      cudaMemset(S->descs.p, 0, sizeof(IndexDesc) * o.max_indexes) != cudaSuccess) {
+    set_error("device control block initialisation failed");
+    return fail(HSDL_ERR_CUDA);
+  }
+  S->slots.resize(o.max_indexes);
+  S->worker = std::thread(worker_main, S);
+  *out = S;
+  return HSDL_OK;
+}
+
+int hsdl_serve_add_index(hsdl_server* S, hsdl_index* idx, int32_t* graph_id) {
+  SRV_ARG(S && idx && graph_id, "null argument");
+  int32_t gid = -1;
+  {
+    std::lock_guard<std::mutex> lk(S->slot_mu);
+    HSDL_TRY(alloc_slot_locked(S, &gid));
+    S->slots[gid].state = 1;
+  }
+  HSDL_CUDA(cudaStreamSynchronize(idx->stream));
+  int rc = write_desc(S, gid, idx, true);
+  std::lock_guard<std::mutex> lk(S->slot_mu);
+  auto& sl = S->slots[gid];
+  if (rc != HSDL_OK) {
+    sl.state = 0;
+    return rc;
+  }
+  hsdl_index_info info;
+  hsdl_index_get_info(idx, &info);
+  sl.idx = idx;
+  sl.owned = false;
+  sl.bytes = info.device_bytes;
+  sl.state = 2;
+  *graph_id = gid;
+  return HSDL_OK;
+}
+
+int hsdl_serve_submit_build(hsdl_server* S, hsdl_graph* g, int32_t K, int32_t* graph_id) {
+  SRV_ARG(S && g && graph_id, "null argument");
+  SRV_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
+  int64_t est = estimate_label_bytes(g->n, g->m2, K);
+  std::lock_guard<std::mutex> lk(S->slot_mu);
+  if (resident_bytes_locked(S) + est > S->opts.budget_bytes) {
+    set_error("build not admitted: resident + pending estimated label bytes would exceed the budget (" +
+              std::to_string(resident_bytes_locked(S) + est) + " > " + std::to_string(S->opts.budget_bytes) + ")");
+    return HSDL_ERR_FULL;
+  }
+  int32_t gid = -1;
+  HSDL_TRY(alloc_slot_locked(S, &gid));
+  auto& sl = S->slots[gid];
+  sl.state = 1;
+  sl.est_bytes = est;
+  sl.error.clear();
+  S->jobs.push_back({gid, g, K});
+  S->slot_cv.notify_all();
+  *graph_id = gid;
+  return HSDL_OK;
+}
+
+int hsdl_serve_graph_state(hsdl_server* S, int32_t graph_id, int32_t* state, int64_t* bytes) {
+  SRV_ARG(S && state, "null argument");
+  SRV_ARG(graph_id >= 0 && graph_id < S->opts.max_indexes, "graph id out of range");
+  std::lock_guard<std::mutex> lk(S->slot_mu);
+  auto& sl = S->slots[graph_id];
+  *state = sl.state;
+  if (bytes) *bytes = sl.state == 2 ? sl.bytes : sl.est_bytes;
+  if (sl.state == 3) set_error(sl.error);
+  return HSDL_OK;
+}
+
+int hsdl_serve_wait_graph(hsdl_server* S, int32_t graph_id, double timeout_s) {
+  SRV_ARG(S, "null server");
+  SRV_ARG(graph_id >= 0 && graph_id < S->opts.max_indexes, "graph id out of range");
+  std::unique_lock<std::mutex> lk(S->slot_mu);
+  bool done = S->slot_cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                  [&] { return S->slots[graph_id].state != 1; });
+  if (!done) {
+    set_error("build still pending at the timeout");
+    return HSDL_ERR_TIMEOUT;
+  }
+  if (S->slots[graph_id].state == 3) {
+    set_error("build failed: " + S->slots[graph_id].error);
+    return HSDL_ERR_STATE;
+  }
+  if (S->slots[graph_id].state != 2) {
+    set_error("graph slot is not resident");
+    return HSDL_ERR_STATE;
+  }
+  return HSDL_OK;
+}
+
+int hsdl_serve_remove_graph(hsdl_server* S, int32_t graph_id) {
+  SRV_ARG(S, "null server");
+  SRV_ARG(graph_id >= 0 && graph_id < S->opts.max_indexes, "graph id out of range");
+  {
+    std::lock_guard<std::mutex> lk(S->slot_mu);
+    if (S->slots[graph_id].state != 2) {
+      set_error("graph slot is not resident");
+      return HSDL_ERR_STATE;
+    }
+  }
+  HSDL_TRY(write_desc(S, graph_id, nullptr, false));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    HSDL_TRY(drain(S, 30.0));
+  }
+  std::lock_guard<std::mutex> lk(S->slot_mu);
+  auto& sl = S->slots[graph_id];
+  if (sl.owned && sl.idx) hsdl_index_destroy(sl.idx);
+  sl = ServerImpl::Slot{};
+  S->slot_cv.notify_all();
+  return HSDL_OK;
+}
+
+// Publishes n requests; *first_ticket receives the ticket of the first.
+// Blocks while the ring is full (answers not yet read by hsdl_serve_wait).
+int hsdl_serve_submit(hsdl_server* S, int64_t n, const int32_t* g, const int32_t* s, const int32_t* t,
+                      const int32_t* k, int64_t* first_ticket) {
+  SRV_ARG(S && n >= 0 && first_ticket, "bad arguments");
+  SRV_ARG(n == 0 || (g && s && t && k), "null request array");
+  std::lock_guard<std::mutex> lk(S->mu);
+  *first_ticket = (int64_t)S->tail;
+  int64_t done = 0;
+  double t0 = mono_s();
+  while (done < n) {
+    uint64_t room = S->cap - (S->tail - S->consumed);
+    if (room == 0) {
+      if (mono_s() - t0 > 30.0) {
+        set_error("ring full: answers are not being consumed (call hsdl_serve_wait)");
+        return HSDL_ERR_FULL;
+      }
+      HSDL_TRY(launch_if_needed(S));
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
+      continue;
+    }
+    int64_t chunk = std::min<int64_t>(n - done, (int64_t)room);
+    for (int64_t i = 0; i < chunk; i++) {
+      uint64_t tk = S->tail + i;
+      S->ring[tk & S->mask] = make_int4(g[done + i], s[done + i], t[done + i], k[done + i]);
+    }
+    S->tail += chunk;
+    __atomic_store_n(&S->hctl->tail, (unsigned long long)S->tail, __ATOMIC_RELEASE);
+    done += chunk;
+    HSDL_TRY(launch_if_needed(S));
+  }
+  return HSDL_OK;
+}
+
+// Waits for the answers of tickets [first_ticket, first_ticket + n), which
+// must be the oldest unread ones, and copies them out.
+int hsdl_serve_wait(hsdl_server* S, int64_t first_ticket, int64_t n, int32_t* answers, double timeout_s) {
+  SRV_ARG(S && n >= 0 && (n == 0 || answers), "bad arguments");
+  std::lock_guard<std::mutex> lk(S->mu);
+  SRV_ARG((uint64_t)first_ticket == S->consumed, "tickets must be read in order, starting at the oldest unread one");
+  SRV_ARG((uint64_t)(first_ticket + n) <= S->tail, "waiting for tickets that were never submitted");
+  double t0 = mono_s();
+  for (int64_t i = 0; i < n; i++) {
+    uint64_t tk = (uint64_t)first_ticket + i;
+    unsigned long long* slot = S->comp + (tk & S->mask);
+    int spins = 0;
+    for (;;) {
+      unsigned long long v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
+      if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) {
+        answers[i] = (int32_t)(uint32_t)v;
+        break;
+      }
+      if (++spins > 4096) {
+        spins = 0;
+        if (mono_s() - t0 > timeout_s) {
+          set_error("answers not complete at the timeout");
+          return HSDL_ERR_TIMEOUT;
+        }
+        HSDL_TRY(launch_if_needed(S));
+        std::this_thread::yield();
+      }
+    }
+    S->consumed = tk + 1;
+  }
+  return HSDL_OK;
+}
+
+// Open-loop load generator: a producer thread publishes the given requests at
+// Poisson arrival times of rate offered_qps (0 = as fast as the ring allows);
+// a consumer thread reads the answers in order and records each request's
+// latency from its scheduled arrival to the moment its answer is seen.
+int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_result* res) {
+  SRV_ARG(S && o && res, "null argument");
+  SRV_ARG(o->struct_size == (int32_t)sizeof(hsdl_loadgen_opts), "hsdl_loadgen_opts.struct_size mismatch");
+  const int64_t n = o->n;
+  SRV_ARG(n >= 1 && o->g && o->s && o->t && o->k, "bad request arrays");
+  std::lock_guard<std::mutex> lk(S->mu);
+  const uint64_t base = S->tail;
+  SRV_ARG(S->consumed == S->tail, "loadgen needs every earlier answer to be read first");
+  std::vector<int64_t> arrive((size_t)n);
+  {
+    uint64_t z = o->seed ? o->seed : 0x9E3779B97F4A7C15ull;
+    double tcur = 0;
+    for (int64_t i = 0; i < n; i++) {
+      if (o->offered_qps > 0) {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        double u = ((double)(x >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        tcur += -std::log(u) / o->offered_qps;
+      }
+      arrive[i] = (int64_t)(tcur * 1e9);
+    }
+  }
+  std::vector<int32_t> lat_ns((size_t)n);
+  std::atomic<uint64_t> consumed_mirror{S->consumed};
+  std::atomic<int> failed{0};
+  int64_t t_start = mono_ns() + 2000000;  // 2 ms to let both threads start
+  HSDL_TRY(launch_if_needed(S));
+  std::thread producer([&] {
+    int64_t i = 0;
+    while (i < n && !failed.load()) {
+      int64_t now = mono_ns() - t_start;
+      if (now < arrive[i]) continue;
+      uint64_t room = S->cap - (S->tail - consumed_mirror.load(std::memory_order_acquire));
+      if (room == 0) continue;
+      int64_t j = i;
+      while (j < n && (uint64_t)(j - i) < room && arrive[j] <= now && j - i < 4096) {
+        uint64_t tk = S->tail + (j - i);
+        S->ring[tk & S->mask] = make_int4(o->g[j], o->s[j], o->t[j], o->k[j]);
+        j++;
+      }
+      S->tail += (uint64_t)(j - i);
+      __atomic_store_n(&S->hctl->tail, (unsigned long long)S->tail, __ATOMIC_RELEASE);
+      i = j;
+    }
+  });
+  int64_t last_done = 0;
+  int64_t idle_check = 0;
+  for (int64_t i = 0; i < n; i++) {
+    uint64_t tk = base + (uint64_t)i;
+    unsigned long long* slot = S->comp + (tk & S->mask);
+    for (;;) {
+      unsigned long long v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
+      if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) {
+        int64_t now = mono_ns() - t_start;
+        lat_ns[i] = (int32_t)std::min<int64_t>(INT32_MAX, now - arrive[i]);
+        if (o->answers) o->answers[i] = (int32_t)(uint32_t)v;
+        last_done = now;
+        break;
+      }
+      if (++idle_check > (1 << 20)) {
+        idle_check = 0;
+        if (cudaStreamQuery(S->stream) != cudaErrorNotReady) {
+          // the loop returned (idle or error): relaunch
+          S->running = true;
+          if (launch_if_needed(S) != HSDL_OK) {
+            failed = 1;
+            break;
+          }
+        }
+      }
+    }
+    if (failed.load()) break;
+    S->consumed = tk + 1;
+    consumed_mirror.store(S->consumed, std::memory_order_release);
+  }
+  producer.join();
+  if (failed.load()) return HSDL_ERR_CUDA;
+  std::vector<int32_t> sorted(lat_ns);
+  std::sort(sorted.begin(), sorted.end());
+  auto pct = [&](double p) { return sorted[std::min<size_t>(sorted.size() - 1, (size_t)(p * (sorted.size() - 1)))]; };
+  res->completed = n;
+  res->seconds = (double)(last_done - arrive[0]) / 1e9;
+  res->achieved_qps = res->seconds > 0 ? (double)n / res->seconds : 0;
+  res->offered_qps = o->offered_qps;
+  res->p50_us = pct(0.50) / 1e3;
+  res->p90_us = pct(0.90) / 1e3;
+  res->p99_us = pct(0.99) / 1e3;
+  res->p999_us = pct(0.999) / 1e3;
+  res->max_us = sorted.back() / 1e3;
+  return HSDL_OK;
+}
+
+int hsdl_serve_stats(hsdl_server* S, hsdl_serve_counters* st) {
+  SRV_ARG(S && st, "null argument");
+  DevCtl c{};
+  HSDL_CUDA(cudaMemcpyAsync(&c, S->ctl.p, sizeof(c), cudaMemcpyDeviceToHost, S->side));
+  HSDL_CUDA(cudaStreamSynchronize(S->side));
+  std::lock_guard<std::mutex> lk(S->slot_mu);
+  st->submitted = (int64_t)S->tail;
+  st->processed = (int64_t)c.processed;
+  st->bad_requests = (int64_t)c.bad;
+  st->resident_graphs = 0;
+  st->pending_builds = 0;
+  for (auto& s : S->slots) {
+    st->resident_graphs += s.state == 2;
+    st->pending_builds += s.state == 1;
+  }
+  st->resident_bytes = resident_bytes_locked(S);
+  st->builds_done = S->builds_done;
+  st->loop_running = S->running && cudaStreamQuery(S->stream) == cudaErrorNotReady;
+  return HSDL_OK;
+}
+
+int hsdl_serve_destroy(hsdl_server* S) {
+  if (!S) return HSDL_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->slot_mu);
+    S->quit = true;
+  }
+  S->slot_cv.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  if (S->hctl) __atomic_store_n(&S->hctl->stop, 1u, __ATOMIC_RELEASE);
+  if (S->stream) cudaStreamSynchronize(S->stream);
+  for (auto& s : S->slots)
+    if (s.owned && s.idx) hsdl_index_destroy(s.idx);
+  S->ctl.release();
+  S->descs.release();
+  if (S->hctl) cudaFreeHost(S->hctl);
+  if (S->ring) cudaFreeHost(S->ring);
+  if (S->comp) cudaFreeHost(S->comp);
+  if (S->stream) cudaStreamDestroy(S->stream);
+  if (S->side) cudaStreamDestroy(S->side);
+  delete S;
+  return HSDL_OK;
+}
+
+}  // extern "C"

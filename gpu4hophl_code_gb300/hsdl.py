@@ -383,3 +383,102 @@ def gpu_query(L, queries, K: int | None = None):
     t0 = time.perf_counter()
     out = _index_of(L).query(q[:, 0], q[:, 1], q[:, 2])
     return out, time.perf_counter() - t0
+
+
+# ---------------------------------------------------------------------------
+# Serving loop
+# ---------------------------------------------------------------------------
+class Server:
+    """Persistent device-resident serving loop over many resident indexes
+    (hsdl_serve_* in include/hsdl.h)."""
+
+    def __init__(self, ctas: int = 0, ring_log2: int = 22, max_indexes: int = 1024,
+                 budget_bytes: int = 120 << 30, idle_exit_s: float = 0.5):
+        o = N.hsdl_serve_opts()
+        lib().hsdl_serve_opts_default(C.byref(o))
+        o.ctas = ctas
+        o.ring_log2 = ring_log2
+        o.max_indexes = max_indexes
+        o.budget_bytes = budget_bytes
+        o.idle_exit_s = idle_exit_s
+        self._h = C.c_void_p()
+        check(lib().hsdl_serve_create(C.byref(o), C.byref(self._h)))
+        self._keep = {}
+
+    def add_index(self, index: Index) -> int:
+        gid = C.c_int32()
+        check(lib().hsdl_serve_add_index(self._h, index.handle, C.byref(gid)))
+        self._keep[gid.value] = index
+        return gid.value
+
+    def submit_build(self, graph: Graph, K: int) -> int:
+        gid = C.c_int32()
+        check(lib().hsdl_serve_submit_build(self._h, graph.handle, K, C.byref(gid)))
+        self._keep[gid.value] = graph
+        return gid.value
+
+    def graph_state(self, gid: int):
+        st = C.c_int32()
+        b = C.c_int64()
+        check(lib().hsdl_serve_graph_state(self._h, gid, C.byref(st), C.byref(b)))
+        return st.value, b.value
+
+    def wait_graph(self, gid: int, timeout_s: float = 600.0) -> None:
+        check(lib().hsdl_serve_wait_graph(self._h, gid, timeout_s))
+
+    def remove_graph(self, gid: int) -> None:
+        check(lib().hsdl_serve_remove_graph(self._h, gid))
+        self._keep.pop(gid, None)
+
+    def query(self, g, s, t, k, timeout_s: float = 60.0) -> np.ndarray:
+        """Submits requests and waits for their answers."""
+        g = np.ascontiguousarray(g, np.int32)
+        s = np.ascontiguousarray(s, np.int32)
+        t = np.ascontiguousarray(t, np.int32)
+        k = np.ascontiguousarray(k, np.int32)
+        n = len(s)
+        out = np.zeros(n, np.int32)
+        first = C.c_int64()
+        step = 1 << 20
+        for lo in range(0, n, step):
+            hi = min(n, lo + step)
+            check(lib().hsdl_serve_submit(self._h, hi - lo, _ptr(g[lo:hi]), _ptr(s[lo:hi]), _ptr(t[lo:hi]),
+                                          _ptr(k[lo:hi]), C.byref(first)))
+            check(lib().hsdl_serve_wait(self._h, first.value, hi - lo, _ptr(out[lo:hi]), timeout_s))
+        return out
+
+    def loadgen(self, g, s, t, k, offered_qps: float = 0.0, seed: int = 1, want_answers: bool = True) -> dict:
+        g = np.ascontiguousarray(g, np.int32)
+        s = np.ascontiguousarray(s, np.int32)
+        t = np.ascontiguousarray(t, np.int32)
+        k = np.ascontiguousarray(k, np.int32)
+        ans = np.zeros(len(s), np.int32) if want_answers else None
+        o = N.hsdl_loadgen_opts()
+        o.struct_size = C.sizeof(N.hsdl_loadgen_opts)
+        o.n = len(s)
+        o.g, o.s, o.t, o.k = g.ctypes.data, s.ctypes.data, t.ctypes.data, k.ctypes.data
+        o.answers = ans.ctypes.data if ans is not None else None
+        o.offered_qps = offered_qps
+        o.seed = seed
+        r = N.hsdl_loadgen_result()
+        check(lib().hsdl_serve_loadgen(self._h, C.byref(o), C.byref(r)))
+        res = {f: getattr(r, f) for f, _ in N.hsdl_loadgen_result._fields_}
+        res["answers"] = ans
+        return res
+
+    def stats(self) -> dict:
+        st = N.hsdl_serve_counters()
+        check(lib().hsdl_serve_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in N.hsdl_serve_counters._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            lib().hsdl_serve_destroy(self._h)
+            self._h = C.c_void_p()
+        self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -194,6 +194,74 @@ int hsdl_save_labels(hsdl_index* idx, const char* path);
 int hsdl_load_labels(const char* path, int32_t K, hsdl_index** out);
 int hsdl_index_destroy(hsdl_index* idx);
 
+/* ------------------------------------------------------------------------
+ * Serving loop (no counterpart in the reference, which answers queries one
+ * at a time: two_hop_labels.h:144, Query_mdnd/src/gpu_query.cu:84).  A
+ * persistent kernel answers (graph, s, t, k) requests published into a ring
+ * in pinned host memory, batching across all resident indexes as requests
+ * arrive; index builds run concurrently and are admitted by estimated label
+ * bytes under a budget.  Answers are bit-identical to hsdl_query_batch on
+ * the same index.
+ * ---------------------------------------------------------------------- */
+typedef struct hsdl_server hsdl_server;
+
+typedef struct hsdl_serve_opts {
+  int32_t struct_size;  /* sizeof(hsdl_serve_opts) */
+  int32_t ctas;         /* blocks of the persistent kernel (0 = 2 per SM) */
+  int32_t ring_log2;    /* request/answer ring capacity = 2^ring_log2 */
+  int32_t max_indexes;  /* graph slots */
+  int64_t budget_bytes; /* admission budget for resident + pending label bytes */
+  double idle_exit_s;   /* the loop returns after this long without requests */
+} hsdl_serve_opts;
+
+typedef struct hsdl_loadgen_opts {
+  int32_t struct_size; /* sizeof(hsdl_loadgen_opts) */
+  int32_t reserved;
+  int64_t n;           /* requests */
+  const int32_t* g;    /* graph id, source, target, hop bound per request */
+  const int32_t* s;
+  const int32_t* t;
+  const int32_t* k;
+  int32_t* answers;    /* optional: answers, in request order */
+  double offered_qps;  /* Poisson arrival rate; 0 = as fast as the ring allows */
+  uint64_t seed;
+} hsdl_loadgen_opts;
+
+typedef struct hsdl_loadgen_result {
+  int64_t completed;
+  double seconds;      /* first scheduled arrival to last answer */
+  double achieved_qps;
+  double offered_qps;
+  double p50_us, p90_us, p99_us, p999_us, max_us; /* arrival -> answer seen */
+} hsdl_loadgen_result;
+
+typedef struct hsdl_serve_counters {
+  int64_t submitted, processed, bad_requests;
+  int64_t resident_graphs, pending_builds, resident_bytes, builds_done;
+  int32_t loop_running;
+  int32_t reserved;
+} hsdl_serve_counters;
+
+void hsdl_serve_opts_default(hsdl_serve_opts* opts);
+int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out);
+/* Registers a built index (the caller keeps it alive) as a graph slot. */
+int hsdl_serve_add_index(hsdl_server* srv, hsdl_index* idx, int32_t* graph_id);
+/* Queues a build of g (kept alive by the caller until the build completes);
+ * HSDL_ERR_FULL if its estimated label bytes do not fit the budget. */
+int hsdl_serve_submit_build(hsdl_server* srv, hsdl_graph* g, int32_t K, int32_t* graph_id);
+/* state: 0 free, 1 building, 2 resident, 3 failed; bytes: resident or estimated */
+int hsdl_serve_graph_state(hsdl_server* srv, int32_t graph_id, int32_t* state, int64_t* bytes);
+int hsdl_serve_wait_graph(hsdl_server* srv, int32_t graph_id, double timeout_s);
+int hsdl_serve_remove_graph(hsdl_server* srv, int32_t graph_id);
+/* Publishes n requests (g[i], s[i], t[i], k[i]); tickets are consecutive. */
+int hsdl_serve_submit(hsdl_server* srv, int64_t n, const int32_t* g, const int32_t* s, const int32_t* t,
+                      const int32_t* k, int64_t* first_ticket);
+/* Reads the answers of the oldest unread tickets [first_ticket, +n). */
+int hsdl_serve_wait(hsdl_server* srv, int64_t first_ticket, int64_t n, int32_t* answers, double timeout_s);
+int hsdl_serve_loadgen(hsdl_server* srv, const hsdl_loadgen_opts* opts, hsdl_loadgen_result* result);
+int hsdl_serve_stats(hsdl_server* srv, hsdl_serve_counters* stats);
+int hsdl_serve_destroy(hsdl_server* srv);
+
 #ifdef __cplusplus
 }
 #endif
