@@ -77,8 +77,10 @@ int new_index(hsdl_index** out) {
     return HSDL_ERR_CUDA;
   }
   // the query kernels' error word, allocated here so that no query call allocates
-  int rc = idx->qerr.alloc(1);
-  if (rc == HSDL_OK && cudaMemset(idx->qerr.p, 0, sizeof(unsigned int)) != cudaSuccess) rc = HSDL_ERR_CUDA;
+  int rc = idx->qerr.alloc(1, idx->stream);
+  if (rc == HSDL_OK && cudaMemsetAsync(idx->qerr.p, 0, sizeof(unsigned int), idx->stream) != cudaSuccess)
+    rc = HSDL_ERR_CUDA;
+  if (rc == HSDL_OK && cudaStreamSynchronize(idx->stream) != cudaSuccess) rc = HSDL_ERR_CUDA;
   if (rc != HSDL_OK) {
     cudaStreamDestroy(idx->stream);
     delete idx;
@@ -97,7 +99,10 @@ void free_index(hsdl_index* idx) {
   idx->hd.release();
   idx->par.release();
   idx->qerr.release();
-  if (idx->stream) cudaStreamDestroy(idx->stream);
+  if (idx->stream) {
+    cudaStreamSynchronize(idx->stream);
+    cudaStreamDestroy(idx->stream);
+  }
   delete idx;
 }
 
@@ -147,16 +152,18 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   idx->total = total;
   idx->before = idx->after = total;
   idx->max_row = mr;
-  HSDL_TRY(idx->off.alloc((int64_t)n + 1));
-  HSDL_TRY(idx->hub.alloc(total + kRowPad));
-  HSDL_TRY(idx->hd.alloc(total + kRowPad));
-  HSDL_TRY(idx->par.alloc(total + kRowPad));
-  HSDL_CUDA(cudaMemcpy(idx->off.p, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice));
+  cudaStream_t st = idx->stream;
+  HSDL_TRY(idx->off.alloc((int64_t)n + 1, st));
+  HSDL_TRY(idx->hub.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->par.alloc(total + kRowPad, st));
+  HSDL_CUDA(cudaMemcpyAsync(idx->off.p, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
   if (total > 0) {
-    HSDL_CUDA(cudaMemcpy(idx->hub.p, hub.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
-    HSDL_CUDA(cudaMemcpy(idx->hd.p, hd.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
-    HSDL_CUDA(cudaMemcpy(idx->par.p, par.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice));
+    HSDL_CUDA(cudaMemcpyAsync(idx->hub.p, hub.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemcpyAsync(idx->hd.p, hd.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemcpyAsync(idx->par.p, par.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
   }
+  HSDL_CUDA(cudaStreamSynchronize(st));
   idx->h_off.assign(offsets, offsets + n + 1);
   return HSDL_OK;
 }
@@ -304,8 +311,9 @@ int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, con
     mw = std::max(mw, w[e]);
   }
   g->max_w = mw;
-  int rc = g->rp.alloc((int64_t)n + 1);
-  if (rc == HSDL_OK) rc = g->adj.alloc(std::max<int64_t>(1, g->m2));
+  int rc = g->rp.alloc((int64_t)n + 1, nullptr);
+  if (rc == HSDL_OK) rc = g->adj.alloc(std::max<int64_t>(1, g->m2), nullptr);
+  if (rc == HSDL_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = HSDL_ERR_CUDA;
   if (rc == HSDL_OK) {
     cudaError_t e1 = cudaMemcpy(g->rp.p, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice);
     cudaError_t e2 = g->m2 ? cudaMemcpy(g->adj.p, adj.data(), sizeof(int2) * g->m2, cudaMemcpyHostToDevice)

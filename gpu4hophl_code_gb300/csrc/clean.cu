@@ -196,14 +196,14 @@ int clean_index(hsdl_index_impl* idx) {
   const int grid = sms * 2;
   int64_t gslots = need_slots > smem_slots ? need_slots : 0;
   DevBuf<int32_t> gscratch;
-  if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * stride));
+  if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * stride, st));
   DevBuf<uint8_t> keep;
   DevBuf<int64_t> kept, noff;
   DevBuf<int> next;
-  HSDL_TRY(keep.alloc(std::max<int64_t>(1, idx->total)));
-  HSDL_TRY(kept.alloc((int64_t)n + 1));
-  HSDL_TRY(noff.alloc((int64_t)n + 1));
-  HSDL_TRY(next.alloc(1));
+  HSDL_TRY(keep.alloc(std::max<int64_t>(1, idx->total), st));
+  HSDL_TRY(kept.alloc((int64_t)n + 1, st));
+  HSDL_TRY(noff.alloc((int64_t)n + 1, st));
+  HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
   k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p, stride,
                                              smem_slots, gscratch.p, gslots, next.p);
@@ -214,9 +214,9 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_CUDA(cudaStreamSynchronize(st));
   DevBuf<uint32_t> nhub, nhd;
   DevBuf<int32_t> npar;
-  HSDL_TRY(nhub.alloc(total + kRowPad));
-  HSDL_TRY(nhd.alloc(total + kRowPad));
-  HSDL_TRY(npar.alloc(total + kRowPad));
+  HSDL_TRY(nhub.alloc(total + kRowPad, st));
+  HSDL_TRY(nhd.alloc(total + kRowPad, st));
+  HSDL_TRY(npar.alloc(total + kRowPad, st));
   k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p, keep.p, noff.p, nhub.p,
                                      nhd.p, npar.p);
   HSDL_LAUNCHED();

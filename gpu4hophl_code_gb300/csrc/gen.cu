@@ -510,37 +510,37 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     ~Guard() { f(); }
   } guard{release_all};
 
-  HSDL_TRY(cand.alloc((int64_t)Wmax * n));
+  HSDL_TRY(cand.alloc((int64_t)Wmax * n, st));
   HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)cand.bytes(), st));
-  HSDL_TRY(row_off.alloc(n));
-  HSDL_TRY(row_len.alloc(n));
-  HSDL_TRY(row_cap.alloc(n));
-  HSDL_TRY(cnt.alloc(n));
-  HSDL_TRY(touched.alloc(n));
+  HSDL_TRY(row_off.alloc(n, st));
+  HSDL_TRY(row_len.alloc(n, st));
+  HSDL_TRY(row_cap.alloc(n, st));
+  HSDL_TRY(cnt.alloc(n, st));
+  HSDL_TRY(touched.alloc(n, st));
   HSDL_CUDA(cudaMemsetAsync(row_off.p, 0, (size_t)row_off.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(row_len.p, 0, (size_t)row_len.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(row_cap.p, 0, (size_t)row_cap.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)cnt.bytes(), st));
   int64_t pool_cap = std::max<int64_t>(1 << 20, (int64_t)n * 16);
-  HSDL_TRY(pool_keys.alloc(pool_cap));
-  HSDL_TRY(pool_par.alloc(pool_cap));
+  HSDL_TRY(pool_keys.alloc(pool_cap, st));
+  HSDL_TRY(pool_par.alloc(pool_cap, st));
   int64_t capC = std::max<int64_t>(1 << 20, (int64_t)n * 4);
   auto alloc_lists = [&](int64_t c) -> int {
-    HSDL_TRY(Cl.alloc(c));
-    HSDL_TRY(Fa.alloc(c));
-    HSDL_TRY(Fb.alloc(c));
-    HSDL_TRY(wl_v.alloc(c));
-    HSDL_TRY(wl_par.alloc(c));
-    HSDL_TRY(wl_key.alloc(c));
+    HSDL_TRY(Cl.alloc(c, st));
+    HSDL_TRY(Fa.alloc(c, st));
+    HSDL_TRY(Fb.alloc(c, st));
+    HSDL_TRY(wl_v.alloc(c, st));
+    HSDL_TRY(wl_par.alloc(c, st));
+    HSDL_TRY(wl_key.alloc(c, st));
     return HSDL_OK;
   };
   HSDL_TRY(alloc_lists(capC));
-  HSDL_TRY(tab_off.alloc(Wmax));
-  HSDL_TRY(tab_cap.alloc(Wmax));
+  HSDL_TRY(tab_off.alloc(Wmax, st));
+  HSDL_TRY(tab_cap.alloc(Wmax, st));
   int64_t tab_cap_entries = 1 << 16;
-  HSDL_TRY(tab.alloc(tab_cap_entries * stride));
-  HSDL_TRY(ctr.alloc(1));
-  HSDL_TRY(pool_tail.alloc(1));
+  HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
+  HSDL_TRY(ctr.alloc(1, st));
+  HSDL_TRY(pool_tail.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(pool_tail.p, 0, sizeof(unsigned long long), st));
   Counters hc;
   unsigned long long h_tail = 0;
@@ -559,7 +559,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       int64_t tab_need = (int64_t)hc.tab_total;
       if (tab_need > tab_cap_entries) {
         while (tab_cap_entries < tab_need) tab_cap_entries *= 2;
-        HSDL_TRY(tab.alloc(tab_cap_entries * stride));
+        HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
       }
       if (tab_need > 0) {
         HSDL_CUDA(cudaMemsetAsync(tab.p, 0x7F, (size_t)tab_need * stride * sizeof(int32_t), st));
@@ -631,17 +631,17 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 
   // --- finalize: exact CSR with self labels, rows sorted by key ------------
   DevBuf<int64_t> flen;
-  HSDL_TRY(flen.alloc((int64_t)n + 1));
-  HSDL_TRY(idx->off.alloc((int64_t)n + 1));
+  HSDL_TRY(flen.alloc((int64_t)n + 1, st));
+  HSDL_TRY(idx->off.alloc((int64_t)n + 1, st));
   k_final_len<<<grid, 256, 0, st>>>(n, row_len.p, flen.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(flen.p, idx->off.p, n, st));
   int64_t total = 0;
   HSDL_CUDA(cudaMemcpyAsync(&total, idx->off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
-  HSDL_TRY(idx->hub.alloc(total + kRowPad));
-  HSDL_TRY(idx->hd.alloc(total + kRowPad));
-  HSDL_TRY(idx->par.alloc(total + kRowPad));
+  HSDL_TRY(idx->hub.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->par.alloc(total + kRowPad, st));
   k_final_copy<<<grid * 2, 256, 0, st>>>(n, row_off.p, row_len.p, pool_keys.p, pool_par.p, idx->off.p,
                                          idx->hub.p, idx->hd.p, idx->par.p);
   HSDL_LAUNCHED();

@@ -47,34 +47,37 @@ struct Status {
     }                                                              \
   } while (0)
 
-// A device buffer with accounting; grows by reallocation.
+// A device buffer, stream-ordered: allocated with cudaMallocAsync and freed
+// with cudaFreeAsync on the stream that owns it, so that allocation never
+// synchronises the device (a persistent serving kernel keeps running while a
+// build allocates and frees).  The owning stream must outlive the buffer.
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   int64_t cap = 0;  // elements
-  int alloc(int64_t n) {
+  cudaStream_t st = nullptr;
+  int alloc(int64_t n, cudaStream_t s = nullptr) {
     release();
+    st = s;
     if (n <= 0) return HSDL_OK;
-    HSDL_CUDA(cudaMalloc(&p, (size_t)n * sizeof(T)));
+    HSDL_CUDA(cudaMallocAsync((void**)&p, (size_t)n * sizeof(T), st));
     cap = n;
     return HSDL_OK;
   }
   // grows to at least n elements keeping the first `keep` elements
-  int grow(int64_t n, int64_t keep, cudaStream_t st) {
+  int grow(int64_t n, int64_t keep, cudaStream_t s) {
     if (n <= cap) return HSDL_OK;
     T* q = nullptr;
-    HSDL_CUDA(cudaMalloc(&q, (size_t)n * sizeof(T)));
-    if (keep > 0 && p) HSDL_CUDA(cudaMemcpyAsync(q, p, (size_t)keep * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    if (p) {
-      HSDL_CUDA(cudaStreamSynchronize(st));
-      cudaFree(p);
-    }
+    HSDL_CUDA(cudaMallocAsync((void**)&q, (size_t)n * sizeof(T), s));
+    if (keep > 0 && p) HSDL_CUDA(cudaMemcpyAsync(q, p, (size_t)keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    if (p) HSDL_CUDA(cudaFreeAsync(p, s));
     p = q;
     cap = n;
+    st = s;
     return HSDL_OK;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st);
     p = nullptr;
     cap = 0;
   }

@@ -397,8 +397,9 @@ int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
     set_error("cudaStreamCreate failed");
     return fail(HSDL_ERR_CUDA);
   }
-  int rc = S->ctl.alloc(1);
-  if (rc == HSDL_OK) rc = S->descs.alloc(o.max_indexes);
+  int rc = S->ctl.alloc(1, S->side);
+  if (rc == HSDL_OK) rc = S->descs.alloc(o.max_indexes, S->side);
+  if (rc == HSDL_OK && cudaStreamSynchronize(S->side) != cudaSuccess) rc = HSDL_ERR_CUDA;
   if (rc != HSDL_OK) return fail(rc);
   cudaError_t e = cudaHostAlloc((void**)&S->hctl, sizeof(HostCtl), cudaHostAllocMapped | cudaHostAllocPortable);
   if (e == cudaSuccess)
@@ -730,6 +731,7 @@ int hsdl_serve_destroy(hsdl_server* S) {
     if (s.owned && s.idx) hsdl_index_destroy(s.idx);
   S->ctl.release();
   S->descs.release();
+  if (S->side) cudaStreamSynchronize(S->side);
   if (S->hctl) cudaFreeHost(S->hctl);
   if (S->ring) cudaFreeHost(S->ring);
   if (S->comp) cudaFreeHost(S->comp);
