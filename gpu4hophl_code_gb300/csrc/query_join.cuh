@@ -67,6 +67,25 @@ __device__ inline long long lane_merge(const uint32_t* A, int la, const uint32_t
   return best;
 }
 
+// TMA bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, multiple of 16).
+__device__ inline void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Prefetches the 16-byte aligned spans holding rows s and t of the hub array
+// into L2 (one lane issues).  The hub array carries padding so the spans stay
+// inside the allocation.
+__device__ inline void prefetch_rows(const int64_t* __restrict__ off, const uint32_t* __restrict__ hub, int32_t n,
+                                     int s, int t) {
+  if (s < 0 || s >= n || t < 0 || t >= n || s == t) return;
+  const int64_t r[2] = {s, t};
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    int64_t a = off[r[i]] & ~(int64_t)3, b = (off[r[i] + 1] + 3) & ~(int64_t)3;
+    if (b > a) prefetch_l2(hub + a, (uint32_t)(b - a) * 4u);
+  }
+}
+
 // Checks that decide an answer without a join; returns true and sets *ans.
 __device__ inline bool trivial_answer(int32_t n, int s, int t, int k, int32_t* ans) {
   if (s < 0 || s >= n || t < 0 || t >= n) {

@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
                                                unsigned long long* comp, unsigned long long mask,
                                                const IndexDesc* descs, int32_t max_idx, long long idle_ns) {
   const int lane = lane_id();
+  const unsigned long long warps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   long long idle_start = globaltimer_ns();
   for (;;) {
     unsigned long long tail = 0, h = 0;
@@ -109,7 +110,10 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       tail = ld_acquire_sys(&hctl->tail);
       h = *(volatile unsigned long long*)&ctl->head;
       if (h < tail) {
-        cnt = (int)min((unsigned long long)32, tail - h);
+        // claim an even share of the backlog (1..32): light load keeps batches
+        // small so no request waits behind many others; heavy load batches
+        unsigned long long share = (tail - h + warps - 1) / warps;
+        cnt = (int)min((unsigned long long)32, max(1ull, share));
         ok = atomicCAS(&ctl->head, h, h + cnt) == h;
       }
     }
@@ -119,25 +123,33 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       cnt = __shfl_sync(0xffffffffu, cnt, 0);
       int4 r = make_int4(-1, 0, 0, 0);
       if (lane < cnt) r = ld_volatile_v4(ring + ((h + lane) & mask));
+      // every lane looks up its own request's index and prefetches its two
+      // rows into L2; the warp then answers the requests one by one
+      IndexDesc d{nullptr, nullptr, nullptr, 0, 0};
+      if (lane < cnt && r.x >= 0 && r.x < max_idx) {
+        d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
+        d.hub = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hub);
+        d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hd);
+        d.n = __ldcg(&descs[r.x].n);
+        d.valid = __ldcg(&descs[r.x].valid);
+        if (d.valid) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
+      }
       int32_t mine = INT_MAX;
       for (int j = 0; j < cnt; j++) {
-        const int g = __shfl_sync(0xffffffffu, r.x, j);
         const int s = __shfl_sync(0xffffffffu, r.y, j);
         const int t = __shfl_sync(0xffffffffu, r.z, j);
         const int k = __shfl_sync(0xffffffffu, r.w, j);
+        const int valid = __shfl_sync(0xffffffffu, d.valid, j);
         int32_t ans = INT_MAX;
-        bool valid = g >= 0 && g < max_idx;
-        IndexDesc d;
         if (valid) {
-          d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[g].off);
-          d.hub = (const uint32_t*)__ldcg((const unsigned long long*)&descs[g].hub);
-          d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[g].hd);
-          d.n = __ldcg(&descs[g].n);
-          d.valid = __ldcg(&descs[g].valid);
-          valid = d.valid != 0;
+          const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
+          const uint32_t* hb = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hub, j);
+          const uint32_t* hx = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hd, j);
+          const int n = __shfl_sync(0xffffffffu, d.n, j);
+          ans = warp_query(n, off, hb, hx, s, t, k);
+        } else if (lane == 0) {
+          atomicAdd(&ctl->bad, 1ull);
         }
-        if (valid) ans = warp_query(d.n, d.off, d.hub, d.hd, s, t, k);
-        else if (lane == 0) atomicAdd(&ctl->bad, 1ull);
         if (lane == j) mine = ans;
       }
       if (lane < cnt) {
