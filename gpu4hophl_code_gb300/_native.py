@@ -71,6 +71,11 @@ class hsdl_serve_counters(C.Structure):
                 ("builds_done", C.c_int64), ("loop_running", C.c_int32), ("reserved", C.c_int32)]
 
 
+class hsdl_query_tuning(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("block_threads", C.c_int32), ("prefetch_ahead", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -105,6 +110,8 @@ SIGNATURES = {
     "hsdl_save_labels": (C.c_int, [P, C.c_char_p]),
     "hsdl_load_labels": (C.c_int, [C.c_char_p, I32, PP]),
     "hsdl_index_destroy": (C.c_int, [P]),
+    "hsdl_set_query_tuning": (C.c_int, [P, C.POINTER(hsdl_query_tuning)]),
+    "hsdl_get_query_tuning": (C.c_int, [P, C.POINTER(hsdl_query_tuning)]),
     "hsdl_serve_opts_default": (None, [C.POINTER(hsdl_serve_opts)]),
     "hsdl_serve_create": (C.c_int, [C.POINTER(hsdl_serve_opts), PP]),
     "hsdl_serve_add_index": (C.c_int, [P, P, C.POINTER(I32)]),

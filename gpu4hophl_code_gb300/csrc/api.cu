@@ -617,6 +617,25 @@ int hsdl_load_labels(const char* path, int32_t K, hsdl_index** out) {
   return hsdl_import((int32_t)V, K, off.data(), lab.empty() ? nullptr : lab.data(), out);
 }
 
+int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* t) {
+  HSDL_CHECK_ARG(idx && t && t->struct_size == (int32_t)sizeof(hsdl_query_tuning), "bad tuning argument");
+  HSDL_CHECK_ARG(t->block_threads >= 32 && t->block_threads <= 1024 && t->block_threads % 32 == 0,
+                 "block_threads must be a multiple of 32 in [32, 1024]");
+  HSDL_CHECK_ARG(t->prefetch_ahead >= 0 && t->prefetch_ahead <= 8, "prefetch_ahead must be in [0, 8]");
+  idx->q_threads = t->block_threads;
+  idx->q_ahead = t->prefetch_ahead;
+  return HSDL_OK;
+}
+
+int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* t) {
+  HSDL_CHECK_ARG(idx && t, "null argument");
+  t->struct_size = (int32_t)sizeof(hsdl_query_tuning);
+  t->block_threads = idx->q_threads;
+  t->prefetch_ahead = idx->q_ahead;
+  t->reserved = 0;
+  return HSDL_OK;
+}
+
 int hsdl_index_destroy(hsdl_index* idx) {
   free_index(idx);
   return HSDL_OK;

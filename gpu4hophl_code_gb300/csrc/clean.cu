@@ -193,7 +193,7 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_CUDA(cudaFuncSetAttribute(k_clean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t need_slots = 8;
   while (need_slots < 2 * idx->max_row) need_slots <<= 1;
-  const int grid = sms * 2;
+  const int grid = sms * resident_blocks(k_clean, kCleanThreads, smem);
   int64_t gslots = need_slots > smem_slots ? need_slots : 0;
   DevBuf<int32_t> gscratch;
   if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * stride, st));

@@ -545,7 +545,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   Counters hc;
   unsigned long long h_tail = 0;
 
-  const int grid = sms * 4;
+  // grids of exactly one resident wave per kernel (grid-stride loops inside)
+  const int grid = sms * resident_blocks(k_scatter, 256);
+  const int g_expand = sms * resident_blocks(k_expand, kThreads);
+  const int g_prune = sms * resident_blocks(k_prune, kThreads);
   for (size_t wv = 0; wv + 1 < bounds.size(); wv++) {
     const int32_t s_hub = bounds[wv], W = bounds[wv + 1] - bounds[wv];
     for (int attempt = 0;; attempt++) {
@@ -572,11 +575,11 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       for (int32_t h = 1; h <= K; h++) {
         int4* Fin = (h & 1) ? Fa.p : Fb.p;
         int4* Fout = (h & 1) ? Fb.p : Fa.p;
-        k_expand<<<grid, kThreads, 0, st>>>(n, h, s_hub, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+        k_expand<<<g_expand, kThreads, 0, st>>>(n, h, s_hub, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
         HSDL_LAUNCHED();
         k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
         HSDL_LAUNCHED();
-        k_prune<<<sms * 8, kThreads, 0, st>>>(n, h, K, s_hub, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p,
+        k_prune<<<g_prune, kThreads, 0, st>>>(n, h, K, s_hub, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p,
                                               tab_off.p, tab_cap.p, tab.p, stride, Fout, wl_v.p, wl_key.p,
                                               wl_par.p, ctr.p);
         HSDL_LAUNCHED();

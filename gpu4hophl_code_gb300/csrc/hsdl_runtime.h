@@ -107,6 +107,8 @@ struct hsdl_index_impl {
   DevBuf<uint32_t> hd;    // hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
+  int32_t q_threads = 256;    // query kernel: threads per block
+  int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;
@@ -116,6 +118,15 @@ struct hsdl_index_impl {
 };
 
 int device_sm_count();
+// Blocks of `kernel` (with `threads` threads and `smem` dynamic shared memory)
+// that fit on one SM at once; grids are sized as SMs x this, so that a
+// grid-stride loop runs in a single wave.
+template <class K>
+int resident_blocks(K kernel, int threads, size_t smem = 0) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
 int max_row_length(hsdl_index_impl* idx, int64_t* out);  // recomputes from h_off
 
 // kernels / stages implemented in the .cu files

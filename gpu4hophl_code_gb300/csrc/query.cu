@@ -22,25 +22,22 @@ namespace hsdl {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kAhead = 2;  // queries prefetched ahead per warp
-
-__global__ void __launch_bounds__(kThreads) k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs,
-                                                    const int32_t* __restrict__ qt, const int32_t* __restrict__ qk,
-                                                    const int64_t* __restrict__ off,
-                                                    const uint32_t* __restrict__ hub,
-                                                    const uint32_t* __restrict__ hd, int32_t* __restrict__ out) {
+// Each warp answers its queries in grid-stride order; `ahead` > 0 makes lane
+// 0 prefetch the rows of the query `ahead` strides further on into L2.
+__global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
+                        const int32_t* __restrict__ qk, const int64_t* __restrict__ off,
+                        const uint32_t* __restrict__ hub, const uint32_t* __restrict__ hd, int32_t* __restrict__ out,
+                        int ahead) {
   const int lane = lane_id();
   const int64_t step = ((int64_t)gridDim.x * blockDim.x) >> 5;
   int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // prime: prefetch the rows of the first kAhead queries of this warp
-  if (lane < kAhead) {
+  if (ahead > 0 && lane < ahead) {
     int64_t p = q + lane * step;
     if (p < nq) prefetch_rows(off, hub, n, qs[p], qt[p]);
   }
   for (; q < nq; q += step) {
-    if (lane == 0) {
-      int64_t p = q + kAhead * step;
+    if (ahead > 0 && lane == 0) {
+      int64_t p = q + ahead * step;
       if (p < nq) prefetch_rows(off, hub, n, qs[p], qt[p]);
     }
     const int32_t ans = warp_query(n, off, hub, hd, qs[q], qt[q], qk[q]);
@@ -54,10 +51,11 @@ int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
                  int32_t* out, cudaStream_t st) {
   if (nq <= 0) return HSDL_OK;
   const int sms = device_sm_count();
-  int64_t blocks = (nq * 32 + kThreads - 1) / kThreads;
-  int64_t max_blocks = (int64_t)sms * 8;
-  k_query<<<(unsigned)std::min(blocks, max_blocks), kThreads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p, idx->hub.p,
-                                                                        idx->hd.p, out);
+  const int threads = idx->q_threads;
+  int64_t blocks = (nq * 32 + threads - 1) / threads;
+  int64_t max_blocks = (int64_t)sms * resident_blocks(k_query, threads);
+  k_query<<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p, idx->hub.p,
+                                                                       idx->hd.p, out, idx->q_ahead);
   HSDL_LAUNCHED();
   return HSDL_OK;
 }

@@ -62,6 +62,7 @@ struct DevCtl {
   unsigned long long bad;        // requests naming no resident graph
   unsigned int exit_reason;      // 1 idle, 2 stop
   unsigned int pad;
+  unsigned long long dev_tail;   // device-side mirror of the host's tail
 };
 
 struct HostCtl {
@@ -97,17 +98,55 @@ __device__ inline long long globaltimer_ns() {
   return t;
 }
 
+__device__ inline unsigned long long ld_acquire_gpu(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release_gpu(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
+  return *(const volatile unsigned int*)p;
+}
+
+// Warp 0 of block 0 is the dispatcher: it alone polls the host's tail and stop
+// flag over the host link and mirrors them into device memory, and it decides
+// the idle exit.  All other warps claim, answer and complete requests.
 __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
                                                unsigned long long* comp, unsigned long long mask,
                                                const IndexDesc* descs, int32_t max_idx, long long idle_ns) {
   const int lane = lane_id();
-  const unsigned long long warps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-  long long idle_start = globaltimer_ns();
+  const bool dispatcher = blockIdx.x == 0 && (threadIdx.x >> 5) == 0;
+  if (dispatcher) {
+    if (lane != 0) return;
+    unsigned long long last = ld_acquire_gpu(&ctl->dev_tail);
+    long long idle_start = globaltimer_ns();
+    for (;;) {
+      const unsigned long long t = ld_acquire_sys(&hctl->tail);
+      if (t != last) {
+        st_release_gpu(&ctl->dev_tail, t);
+        last = t;
+        idle_start = globaltimer_ns();
+      }
+      if (ld_volatile_u32(&hctl->stop)) {
+        atomicMax(&ctl->exit_reason, 2u);
+        return;
+      }
+      if (globaltimer_ns() - idle_start > idle_ns &&
+          *(volatile unsigned long long*)&ctl->processed >= last) {
+        atomicMax(&ctl->exit_reason, 1u);
+        return;
+      }
+      __nanosleep(100);
+    }
+  }
+  const unsigned long long warps = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
   for (;;) {
     unsigned long long tail = 0, h = 0;
     int ok = 0, cnt = 0;
     if (lane == 0) {
-      tail = ld_acquire_sys(&hctl->tail);
+      tail = ld_acquire_gpu(&ctl->dev_tail);
       h = *(volatile unsigned long long*)&ctl->head;
       if (h < tail) {
         // claim an even share of the backlog (1..32): light load keeps batches
@@ -132,7 +171,7 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hd);
         d.n = __ldcg(&descs[r.x].n);
         d.valid = __ldcg(&descs[r.x].valid);
-        if (d.valid) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
+        if (d.valid && cnt > 1) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
       }
       int32_t mine = INT_MAX;
       for (int j = 0; j < cnt; j++) {
@@ -152,31 +191,23 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         }
         if (lane == j) mine = ans;
       }
+      // one 8-byte store per answer carries its ticket, so the host needs no
+      // ordering between slots
       if (lane < cnt) {
         unsigned long long tk = h + lane;
         st_relaxed_sys(comp + (tk & mask), ((unsigned long long)(uint32_t)(tk + 1) << 32) | (uint32_t)mine);
       }
-      __threadfence_system();
       if (lane == 0) atomicAdd(&ctl->processed, (unsigned long long)cnt);
-      idle_start = globaltimer_ns();
       continue;
-    }
-    // nothing claimed: stop, idle exit or back off
-    unsigned int stop = 0;
-    if (lane == 0) stop = ld_volatile_u32(&hctl->stop);
-    stop = __shfl_sync(0xffffffffu, stop, 0);
-    if (stop) {
-      if (lane == 0) atomicMax(&ctl->exit_reason, 2u);
-      return;
     }
     tail = __shfl_sync(0xffffffffu, tail, 0);
     h = __shfl_sync(0xffffffffu, h, 0);
     if (h >= tail) {
-      if (globaltimer_ns() - idle_start > idle_ns) {
-        if (lane == 0) atomicMax(&ctl->exit_reason, 1u);
-        return;
-      }
-      __nanosleep(200);
+      unsigned int ex = 0;
+      if (lane == 0) ex = ld_volatile_dev_u32(&ctl->exit_reason);
+      ex = __shfl_sync(0xffffffffu, ex, 0);
+      if (ex) return;  // the dispatcher left: idle or stop, nothing published is unclaimed
+      __nanosleep(100);
     }
   }
 }

@@ -157,6 +157,18 @@ int hsdl_query_batch_device(hsdl_index* idx, int64_t nq, const int32_t* d_s, con
 int hsdl_query_batch_static(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                             int32_t* out);
 
+/* Launch parameters of the query kernel for one index (the autotuner's
+ * knobs): threads per block (multiple of 32, 32..1024) and how many queries
+ * ahead each warp prefetches rows into L2 (0..8). */
+typedef struct hsdl_query_tuning {
+  int32_t struct_size;
+  int32_t block_threads;
+  int32_t prefetch_ahead;
+  int32_t reserved;
+} hsdl_query_tuning;
+int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* tuning);
+int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* tuning);
+
 /* Path extraction: hop_constrained_extract_shortest_path
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:224).  Writes
  * edges as (a,b) pairs into edges[2*cap]; *n_edges = count. */
