@@ -111,14 +111,20 @@ __device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
 }
 
 // Warp 0 of block 0 is the dispatcher: it alone polls the host's tail and stop
-// flag over the host link and mirrors them into device memory, and it decides
-// the idle exit.  All other warps claim, answer and complete requests.
+// flag over the host link and mirrors the tail into device memory, and it
+// decides the idle exit.  The other W warps are workers with a fixed share of
+// the tickets: ticket base + w + j*W belongs to worker w, so no two warps ever
+// contend for a request.  A worker answers all of its published tickets (up
+// to 32 at once: their requests are read in parallel and their rows
+// prefetched), one after another, and writes each answer with its ticket into
+// the completion ring.
 __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
                                                unsigned long long* comp, unsigned long long mask,
-                                               const IndexDesc* descs, int32_t max_idx, long long idle_ns) {
+                                               const IndexDesc* descs, int32_t max_idx, long long idle_ns,
+                                               unsigned long long base) {
   const int lane = lane_id();
-  const bool dispatcher = blockIdx.x == 0 && (threadIdx.x >> 5) == 0;
-  if (dispatcher) {
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (gw == 0) {
     if (lane != 0) return;
     unsigned long long last = ld_acquire_gpu(&ctl->dev_tail);
     long long idle_start = globaltimer_ns();
@@ -133,37 +139,28 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         atomicMax(&ctl->exit_reason, 2u);
         return;
       }
-      if (globaltimer_ns() - idle_start > idle_ns &&
-          *(volatile unsigned long long*)&ctl->processed >= last) {
+      if (globaltimer_ns() - idle_start > idle_ns && *(volatile unsigned long long*)&ctl->processed >= last) {
         atomicMax(&ctl->exit_reason, 1u);
         return;
       }
       __nanosleep(100);
     }
   }
-  const unsigned long long warps = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
+  const unsigned long long W = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
+  unsigned long long next = base + (unsigned long long)(gw - 1);
+  unsigned int backoff = 64;
   for (;;) {
-    unsigned long long tail = 0, h = 0;
-    int ok = 0, cnt = 0;
-    if (lane == 0) {
-      tail = ld_acquire_gpu(&ctl->dev_tail);
-      h = *(volatile unsigned long long*)&ctl->head;
-      if (h < tail) {
-        // claim an even share of the backlog (1..32): light load keeps batches
-        // small so no request waits behind many others; heavy load batches
-        unsigned long long share = (tail - h + warps - 1) / warps;
-        cnt = (int)min((unsigned long long)32, max(1ull, share));
-        ok = atomicCAS(&ctl->head, h, h + cnt) == h;
-      }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (ok) {
-      h = __shfl_sync(0xffffffffu, h, 0);
-      cnt = __shfl_sync(0xffffffffu, cnt, 0);
+    unsigned long long tail = 0;
+    if (lane == 0) tail = ld_acquire_gpu(&ctl->dev_tail);
+    tail = __shfl_sync(0xffffffffu, tail, 0);
+    if (next < tail) {
+      backoff = 64;
+      const int cnt = (int)min((unsigned long long)32, (tail - next + W - 1) / W);
+      const unsigned long long mine_tk = next + (unsigned long long)lane * W;
       int4 r = make_int4(-1, 0, 0, 0);
-      if (lane < cnt) r = ld_volatile_v4(ring + ((h + lane) & mask));
-      // every lane looks up its own request's index and prefetches its two
-      // rows into L2; the warp then answers the requests one by one
+      if (lane < cnt) r = ld_volatile_v4(ring + (mine_tk & mask));
+      // every lane looks up its own request's index (and prefetches its rows
+      // into L2 when the warp has several to answer)
       IndexDesc d{nullptr, nullptr, nullptr, 0, 0};
       if (lane < cnt && r.x >= 0 && r.x < max_idx) {
         d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
@@ -193,22 +190,18 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       }
       // one 8-byte store per answer carries its ticket, so the host needs no
       // ordering between slots
-      if (lane < cnt) {
-        unsigned long long tk = h + lane;
-        st_relaxed_sys(comp + (tk & mask), ((unsigned long long)(uint32_t)(tk + 1) << 32) | (uint32_t)mine);
-      }
+      if (lane < cnt)
+        st_relaxed_sys(comp + (mine_tk & mask), ((unsigned long long)(uint32_t)(mine_tk + 1) << 32) | (uint32_t)mine);
       if (lane == 0) atomicAdd(&ctl->processed, (unsigned long long)cnt);
+      next += (unsigned long long)cnt * W;
       continue;
     }
-    tail = __shfl_sync(0xffffffffu, tail, 0);
-    h = __shfl_sync(0xffffffffu, h, 0);
-    if (h >= tail) {
-      unsigned int ex = 0;
-      if (lane == 0) ex = ld_volatile_dev_u32(&ctl->exit_reason);
-      ex = __shfl_sync(0xffffffffu, ex, 0);
-      if (ex) return;  // the dispatcher left: idle or stop, nothing published is unclaimed
-      __nanosleep(100);
-    }
+    unsigned int ex = 0;
+    if (lane == 0) ex = ld_volatile_dev_u32(&ctl->exit_reason);
+    ex = __shfl_sync(0xffffffffu, ex, 0);
+    if (ex) return;  // the dispatcher left: every published ticket of this warp is answered
+    __nanosleep(backoff);
+    backoff = min(backoff * 2, 2048u);
   }
 }
 
@@ -275,10 +268,16 @@ int launch_if_needed(ServerImpl* S) {
     }
     S->running = false;  // it returned (idle)
   }
+  // tickets below `processed` are all answered and none above it is: the new
+  // kernel's workers start there
+  unsigned long long processed = 0;
+  HSDL_CUDA(cudaMemcpyAsync(&processed, &S->ctl.p->processed, sizeof(processed), cudaMemcpyDeviceToHost,
+                            S->stream));
   HSDL_CUDA(cudaMemsetAsync(&S->ctl.p->exit_reason, 0, sizeof(unsigned int), S->stream));
+  HSDL_CUDA(cudaStreamSynchronize(S->stream));
   long long idle_ns = (long long)(S->opts.idle_exit_s * 1e9);
   k_serve<<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
-                                               S->descs.p, S->opts.max_indexes, idle_ns);
+                                               S->descs.p, S->opts.max_indexes, idle_ns, processed);
   HSDL_LAUNCHED();
   S->running = true;
   return HSDL_OK;
