@@ -113,11 +113,12 @@ __device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
 // Warp 0 of block 0 is the dispatcher: it alone polls the host's tail and stop
 // flag over the host link and mirrors the tail into device memory, and it
 // decides the idle exit.  The other W warps are workers with a fixed share of
-// the tickets: ticket base + w + j*W belongs to worker w, so no two warps ever
-// contend for a request.  A worker answers all of its published tickets (up
-// to 32 at once: their requests are read in parallel and their rows
-// prefetched), one after another, and writes each answer with its ticket into
-// the completion ring.
+// the tickets, in chunks of 8 (one 64-byte line of the completion ring):
+// chunk c = (ticket - base) / 8 belongs to worker c mod W, so no two warps
+// contend for a request and every completion line is written once, by one
+// coalesced store.  A worker answers all of its published tickets (up to 32
+// at once: their requests are read in parallel and their rows prefetched),
+// one after another.
 __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
                                                unsigned long long* comp, unsigned long long mask,
                                                const IndexDesc* descs, int32_t max_idx, long long idle_ns,
@@ -147,16 +148,20 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
     }
   }
   const unsigned long long W = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
-  unsigned long long next = base + (unsigned long long)(gw - 1);
+  const unsigned long long w = (unsigned long long)(gw - 1);
+  unsigned long long done = 0;  // tickets of this worker answered so far
   unsigned int backoff = 64;
   for (;;) {
     unsigned long long tail = 0;
     if (lane == 0) tail = ld_acquire_gpu(&ctl->dev_tail);
     tail = __shfl_sync(0xffffffffu, tail, 0);
-    if (next < tail) {
+    // this worker's (done + lane)-th ticket
+    const unsigned long long kk = done + (unsigned long long)lane;
+    const unsigned long long mine_tk = base + 8ull * (w + (kk >> 3) * W) + (kk & 7ull);
+    const unsigned int avail = __ballot_sync(0xffffffffu, mine_tk < tail);  // a prefix: tickets increase with lane
+    if (avail) {
       backoff = 64;
-      const int cnt = (int)min((unsigned long long)32, (tail - next + W - 1) / W);
-      const unsigned long long mine_tk = next + (unsigned long long)lane * W;
+      const int cnt = __popc(avail);
       int4 r = make_int4(-1, 0, 0, 0);
       if (lane < cnt) r = ld_volatile_v4(ring + (mine_tk & mask));
       // every lane looks up its own request's index (and prefetches its rows
@@ -193,7 +198,7 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       if (lane < cnt)
         st_relaxed_sys(comp + (mine_tk & mask), ((unsigned long long)(uint32_t)(mine_tk + 1) << 32) | (uint32_t)mine);
       if (lane == 0) atomicAdd(&ctl->processed, (unsigned long long)cnt);
-      next += (unsigned long long)cnt * W;
+      done += (unsigned long long)cnt;
       continue;
     }
     unsigned int ex = 0;
@@ -696,6 +701,11 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
   for (int64_t i = 0; i < n; i++) {
     uint64_t tk = base + (uint64_t)i;
     unsigned long long* slot = S->comp + (tk & S->mask);
+    if ((tk & 7) == 0) {
+      // completion lines are written by the GPU over the host link; keep
+      // several line fetches in flight instead of one miss at a time
+      for (int a = 1; a <= 16; a++) __builtin_prefetch(S->comp + ((tk + 8ull * (uint64_t)(8 + a)) & S->mask), 0, 0);
+    }
     for (;;) {
       unsigned long long v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
       if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) {
