@@ -50,7 +50,8 @@ class hsdl_index_info(C.Structure):
 
 class hsdl_serve_opts(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("ctas", C.c_int32), ("ring_log2", C.c_int32),
-                ("max_indexes", C.c_int32), ("budget_bytes", C.c_int64), ("idle_exit_s", C.c_double)]
+                ("max_indexes", C.c_int32), ("budget_bytes", C.c_int64), ("idle_exit_s", C.c_double),
+                ("lanes_per_query", C.c_int32), ("reserved", C.c_int32)]
 
 
 class hsdl_loadgen_opts(C.Structure):
@@ -62,7 +63,8 @@ class hsdl_loadgen_opts(C.Structure):
 class hsdl_loadgen_result(C.Structure):
     _fields_ = [("completed", C.c_int64), ("seconds", C.c_double), ("achieved_qps", C.c_double),
                 ("offered_qps", C.c_double), ("p50_us", C.c_double), ("p90_us", C.c_double),
-                ("p99_us", C.c_double), ("p999_us", C.c_double), ("max_us", C.c_double)]
+                ("p99_us", C.c_double), ("p999_us", C.c_double), ("max_us", C.c_double),
+                ("ready_frac", C.c_double)]
 
 
 class hsdl_serve_counters(C.Structure):
@@ -73,7 +75,7 @@ class hsdl_serve_counters(C.Structure):
 
 class hsdl_query_tuning(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("block_threads", C.c_int32), ("prefetch_ahead", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("lanes_per_query", C.c_int32)]
 
 
 P = C.c_void_p
@@ -96,6 +98,7 @@ SIGNATURES = {
     "hsdl_validate_csr": (C.c_int, [I32, P, P, P]),
     "hsdl_graph_create": (C.c_int, [I32, P, P, P, PP]),
     "hsdl_graph_destroy": (C.c_int, [P]),
+    "hsdl_group_lp": (C.c_int, [P, I32, I32, P, C.POINTER(I32), C.POINTER(I32)]),
     "hsdl_build_opts_default": (None, [C.POINTER(hsdl_build_opts)]),
     "hsdl_wave_bounds": (C.c_int, [I32, C.POINTER(hsdl_build_opts), P, I32, C.POINTER(I32)]),
     "hsdl_build": (C.c_int, [P, I32, C.POINTER(hsdl_build_opts), PP]),

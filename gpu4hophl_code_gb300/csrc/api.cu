@@ -341,6 +341,14 @@ int hsdl_graph_destroy(hsdl_graph* g) {
   return HSDL_OK;
 }
 
+int hsdl_group_lp(hsdl_graph* g, int32_t max_group, int32_t max_iterations, int32_t* group_of_vertex,
+                  int32_t* num_groups, int32_t* iterations) {
+  HSDL_CHECK_ARG(g && group_of_vertex && num_groups, "null argument");
+  HSDL_CHECK_ARG(max_group >= 1, "max_group must be >= 1");
+  HSDL_CHECK_ARG(max_iterations >= 0, "max_iterations must be >= 0");
+  return group_lp(g, max_group, max_iterations, group_of_vertex, num_groups, iterations);
+}
+
 // ---------------------------------------------------------------------------
 // build / clean
 // ---------------------------------------------------------------------------
@@ -622,8 +630,11 @@ int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* t) {
   HSDL_CHECK_ARG(t->block_threads >= 32 && t->block_threads <= 1024 && t->block_threads % 32 == 0,
                  "block_threads must be a multiple of 32 in [32, 1024]");
   HSDL_CHECK_ARG(t->prefetch_ahead >= 0 && t->prefetch_ahead <= 8, "prefetch_ahead must be in [0, 8]");
+  HSDL_CHECK_ARG(t->lanes_per_query == 8 || t->lanes_per_query == 16 || t->lanes_per_query == 32,
+                 "lanes_per_query must be 8, 16 or 32");
   idx->q_threads = t->block_threads;
   idx->q_ahead = t->prefetch_ahead;
+  idx->q_lanes = t->lanes_per_query;
   return HSDL_OK;
 }
 
@@ -632,7 +643,7 @@ int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* t) {
   t->struct_size = (int32_t)sizeof(hsdl_query_tuning);
   t->block_threads = idx->q_threads;
   t->prefetch_ahead = idx->q_ahead;
-  t->reserved = 0;
+  t->lanes_per_query = idx->q_lanes;
   return HSDL_OK;
 }
 

@@ -107,7 +107,8 @@ struct hsdl_index_impl {
   DevBuf<uint32_t> hd;    // hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
-  int32_t q_threads = 256;    // query kernel: threads per block
+  int32_t q_threads = 512;    // query kernel: threads per block
+  int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
@@ -132,6 +133,8 @@ int max_row_length(hsdl_index_impl* idx, int64_t* out);  // recomputes from h_of
 // kernels / stages implemented in the .cu files
 int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx);
 int clean_index(hsdl_index_impl* idx);
+int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,
+             int32_t* iterations_run);
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st);
 int query_error(hsdl_index_impl* idx);  // HSDL_ERR_TIMEOUT (and clears) if a query kernel flagged one

@@ -1,0 +1,309 @@
+// Label-propagation vertex grouping (groups of at most G_max vertices).
+//
+// Reference: generate_Group_CDLP
+// (Hybrid_Generation_Clean/include/vgroup/CDLP_group.cuh:20-107) over CDLP_GPU
+// (Hybrid_Generation_Clean/include/vgroup/CDLP/GPU_Community_Detection.cuh:
+// 29-213): labels start as vertex ids; each iteration gathers the labels of
+// every vertex's neighbours (LabelPropagation, :29-42), sorts them per vertex
+// (cub::DeviceSegmentedSort, :142,173) and takes the most frequent label whose
+// community is not full (Get_New_Label, :58-91); the host then buckets by
+// label, greedily merges small groups up to G_max (CDLP_group.cuh:56-82) and
+// orders the groups by total degree (:84-100).
+//
+// The reference's size cap is enforced with racy atomics, so its groups
+// change from run to run.  This restatement is deterministic:
+//   1. size[c] = vertices labelled c (exact histogram);
+//   2. every vertex gathers its neighbours' labels, sorts them (warp bitonic
+//      network for rows up to 32, block network in shared memory beyond) and
+//      proposes the most frequent label c with c == own label or
+//      size[c] < G_max, ties to the smaller label (no neighbours: keep);
+//   3. join[c] = vertices proposing c != own label; a label's joiners move
+//      iff size[c] + join[c] <= G_max (all or none), so no group exceeds G_max;
+//   4. stop when nothing moves or after max_iterations.
+// The host merge and ordering then follow the reference's rules exactly.
+#include <algorithm>
+#include <chrono>
+#include <set>
+#include <vector>
+
+#include "hsdl_device.cuh"
+#include "hsdl_runtime.h"
+
+namespace hsdl {
+
+namespace {
+
+constexpr int kLpThreads = 256;
+
+__global__ void k_lp_init(int32_t n, int32_t* __restrict__ label) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+    label[v] = (int32_t)v;
+}
+
+__global__ void k_lp_hist(int32_t n, const int32_t* __restrict__ label, int32_t* __restrict__ size) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&size[label[v]], 1);
+}
+
+// prop[e] = label[col[e]]  (LabelPropagation)
+__global__ void k_lp_gather(int64_t m2, const int2* __restrict__ adj, const int32_t* __restrict__ label,
+                            uint32_t* __restrict__ prop) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m2; e += (int64_t)gridDim.x * blockDim.x)
+    prop[e] = (uint32_t)label[adj[e].x];
+}
+
+// Sorts every row of prop (rows of up to 32 entries; one warp per row).
+__global__ void k_lp_sort_small(int32_t n, const int64_t* __restrict__ rp, uint32_t* __restrict__ prop) {
+  const int lane = lane_id();
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = warp; v < n; v += nwarps) {
+    int64_t lo = rp[v], len = rp[v + 1] - lo;
+    if (len <= 1 || len > 32) continue;
+    uint32_t k = lane < len ? prop[lo + lane] : 0xFFFFFFFFu;
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        uint32_t o = __shfl_xor_sync(0xffffffffu, k, stride);
+        bool up = ((lane & size) == 0);
+        bool lower = ((lane & stride) == 0);
+        if (lower == up ? (o < k) : (o > k)) k = o;
+      }
+    }
+    if (lane < len) prop[lo + lane] = k;
+  }
+}
+
+// Rows longer than 32 (listed in rows[0..*count)): one block per row, bitonic
+// network in shared memory (cap entries) or in a global scratch row.
+__global__ void k_lp_sort_large(const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
+                                const int64_t* __restrict__ rp, uint32_t* __restrict__ prop, int cap,
+                                uint32_t* __restrict__ gscratch, int64_t gcap) {
+  extern __shared__ uint32_t sm_keys[];
+  const int cnt = *count;
+  for (int r = blockIdx.x; r < cnt; r += gridDim.x) {
+    const int v = rows[r];
+    const int64_t lo = rp[v], len = rp[v + 1] - lo;
+    int64_t P = 1;
+    while (P < len) P <<= 1;
+    uint32_t* a = P <= cap ? sm_keys : gscratch + (int64_t)blockIdx.x * gcap;
+    for (int64_t i = threadIdx.x; i < P; i += blockDim.x) a[i] = i < len ? prop[lo + i] : 0xFFFFFFFFu;
+    for (int64_t size = 2; size <= P; size <<= 1) {
+      for (int64_t stride = size >> 1; stride > 0; stride >>= 1) {
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
+          int64_t x = 2 * i - (i & (stride - 1)), y = x + stride;
+          bool up = ((x & size) == 0);
+          uint32_t p = a[x], q = a[y];
+          if ((p > q) == up) {
+            a[x] = q;
+            a[y] = p;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) prop[lo + i] = a[i];
+    __syncthreads();
+  }
+}
+
+__global__ void k_lp_list_rows(int32_t n, const int64_t* __restrict__ rp, int32_t* __restrict__ rows,
+                               int32_t* __restrict__ count) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+    if (rp[v + 1] - rp[v] > 32) rows[atomicAdd(count, 1)] = (int32_t)v;
+}
+
+// Mode of the sorted neighbour labels among eligible labels (Get_New_Label).
+__global__ void k_lp_choose(int32_t n, const int64_t* __restrict__ rp, const uint32_t* __restrict__ prop,
+                            const int32_t* __restrict__ label, const int32_t* __restrict__ size, int32_t gmax,
+                            int32_t* __restrict__ proposed, int32_t* __restrict__ join) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t own = label[v];
+    int32_t best = own;
+    int64_t best_cnt = 0;
+    const int64_t lo = rp[v], hi = rp[v + 1];
+    int64_t i = lo;
+    while (i < hi) {
+      const uint32_t c = prop[i];
+      int64_t j = i + 1;
+      while (j < hi && prop[j] == c) j++;
+      const int64_t cntc = j - i;
+      const bool eligible = (int32_t)c == own || size[c] < gmax;
+      // strictly more, or equal count and smaller label (runs come in
+      // increasing label order, so a later equal count is never smaller)
+      if (eligible && cntc > best_cnt) {
+        best_cnt = cntc;
+        best = (int32_t)c;
+      }
+      i = j;
+    }
+    proposed[v] = best;
+    if (best != own) atomicAdd(&join[best], 1);
+  }
+}
+
+__global__ void k_lp_apply(int32_t n, const int32_t* __restrict__ label, const int32_t* __restrict__ proposed,
+                           const int32_t* __restrict__ size, const int32_t* __restrict__ join, int32_t gmax,
+                           int32_t* __restrict__ out, unsigned long long* changed) {
+  unsigned long long local = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t own = label[v], c = proposed[v];
+    int32_t nl = own;
+    if (c != own && size[c] + join[c] <= gmax) nl = c;
+    out[v] = nl;
+    local += nl != own;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if (lane_id() == 0 && local) atomicAdd(changed, local);
+}
+
+}  // namespace
+
+// Host side of generate_Group_CDLP (CDLP_group.cuh:39-100): bucket by label,
+// merge small groups greedily, order by total degree.
+struct GroupUnit {
+  int64_t id, size;
+  std::vector<int32_t> nodes;
+  bool operator<(const GroupUnit& b) const { return size == b.size ? id < b.id : size < b.size; }
+};
+
+void assemble_groups(int32_t n, const int32_t* label, const int64_t* rp, int32_t gmax,
+                     std::vector<std::vector<int32_t>>& groups) {
+  std::vector<std::vector<int32_t>> buckets((size_t)n);
+  for (int32_t v = 0; v < n; v++) buckets[label[v]].push_back(v);
+  std::vector<std::vector<int32_t>> nonempty;
+  for (auto& b : buckets)
+    if (!b.empty()) nonempty.push_back(std::move(b));
+  std::set<GroupUnit> se;
+  for (size_t g = 0; g < nonempty.size(); g++) se.insert(GroupUnit{(int64_t)g, (int64_t)nonempty[g].size(), nonempty[g]});
+  std::vector<std::vector<int32_t>> after;
+  // take the largest group; merge it with the largest other group that still
+  // fits (CDLP_group.cuh:56-82)
+  while (!se.empty()) {
+    auto it1 = std::prev(se.end());
+    int64_t room = gmax - it1->size;
+    auto it2 = se.upper_bound(GroupUnit{(int64_t)nonempty.size(), room, {}});
+    bool merged = false;
+    if (it2 != se.begin()) {
+      --it2;
+      if (it2 == it1) {
+        if (it2 != se.begin()) {
+          --it2;
+        } else {
+          it2 = se.end();
+        }
+      }
+      if (it2 != se.end() && it2 != it1 && it1->size + it2->size <= gmax) {
+        GroupUnit a = *it1, b = *it2;
+        a.size += b.size;
+        a.nodes.insert(a.nodes.end(), b.nodes.begin(), b.nodes.end());
+        se.erase(it1);
+        se.erase(it2);
+        se.insert(a);
+        merged = true;
+      }
+    }
+    if (!merged) {
+      after.push_back(it1->nodes);
+      se.erase(it1);
+    }
+  }
+  // order by total degree, largest first (ties by position)
+  std::vector<GroupUnit> order;
+  for (size_t g = 0; g < after.size(); g++) {
+    int64_t tot = 0;
+    for (int32_t v : after[g]) tot -= rp[v + 1] - rp[v];
+    order.push_back(GroupUnit{(int64_t)g, tot, after[g]});
+  }
+  std::sort(order.begin(), order.end());
+  groups.clear();
+  for (auto& u : order) groups.push_back(std::move(u.nodes));
+}
+
+int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,
+             int32_t* iterations_run) {
+  const int32_t n = g->n;
+  const int64_t m2 = g->m2;
+  cudaStream_t st = nullptr;
+  HSDL_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  } sg{st};
+  const int sms = device_sm_count();
+  DevBuf<int32_t> label, nlabel, size, join, proposed, rows, count;
+  DevBuf<uint32_t> prop, gscratch;
+  DevBuf<unsigned long long> changed;
+  HSDL_TRY(label.alloc(n, st));
+  HSDL_TRY(nlabel.alloc(n, st));
+  HSDL_TRY(size.alloc(n, st));
+  HSDL_TRY(join.alloc(n, st));
+  HSDL_TRY(proposed.alloc(n, st));
+  HSDL_TRY(rows.alloc(n, st));
+  HSDL_TRY(count.alloc(1, st));
+  HSDL_TRY(prop.alloc(std::max<int64_t>(1, m2), st));
+  HSDL_TRY(changed.alloc(1, st));
+  int64_t maxdeg = 0;
+  for (int32_t v = 0; v < n; v++) maxdeg = std::max(maxdeg, g->h_rp[v + 1] - g->h_rp[v]);
+  const int cap = 16384;  // 64 KB of shared memory per block
+  int64_t P = 1;
+  while (P < maxdeg) P <<= 1;
+  const int large_grid = sms * 2;
+  if (P > cap) HSDL_TRY(gscratch.alloc((int64_t)large_grid * P, st));
+  HSDL_CUDA(cudaFuncSetAttribute(k_lp_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(cap * sizeof(uint32_t))));
+  const int grid = sms * resident_blocks(k_lp_choose, kLpThreads);
+  HSDL_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t), st));
+  k_lp_list_rows<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, rows.p, count.p);
+  HSDL_LAUNCHED();
+  k_lp_init<<<grid, kLpThreads, 0, st>>>(n, label.p);
+  HSDL_LAUNCHED();
+  int32_t it = 0;
+  for (; it < max_iter; it++) {
+    HSDL_CUDA(cudaMemsetAsync(size.p, 0, sizeof(int32_t) * n, st));
+    HSDL_CUDA(cudaMemsetAsync(join.p, 0, sizeof(int32_t) * n, st));
+    HSDL_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(unsigned long long), st));
+    k_lp_hist<<<grid, kLpThreads, 0, st>>>(n, label.p, size.p);
+    HSDL_LAUNCHED();
+    if (m2 > 0) {
+      k_lp_gather<<<grid, kLpThreads, 0, st>>>(m2, g->adj.p, label.p, prop.p);
+      HSDL_LAUNCHED();
+      k_lp_sort_small<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, prop.p);
+      HSDL_LAUNCHED();
+      k_lp_sort_large<<<large_grid, 512, cap * sizeof(uint32_t), st>>>(rows.p, count.p, g->rp.p, prop.p, cap,
+                                                                       gscratch.p, P);
+      HSDL_LAUNCHED();
+    }
+    k_lp_choose<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, prop.p, label.p, size.p, gmax, proposed.p, join.p);
+    HSDL_LAUNCHED();
+    k_lp_apply<<<grid, kLpThreads, 0, st>>>(n, label.p, proposed.p, size.p, join.p, gmax, nlabel.p, changed.p);
+    HSDL_LAUNCHED();
+    std::swap(label.p, nlabel.p);
+    unsigned long long h_changed = 0;
+    HSDL_CUDA(cudaMemcpyAsync(&h_changed, changed.p, sizeof(h_changed), cudaMemcpyDeviceToHost, st));
+    HSDL_CUDA(cudaStreamSynchronize(st));
+    if (h_changed == 0) {
+      it++;
+      break;
+    }
+  }
+  std::vector<int32_t> h_label((size_t)n);
+  HSDL_CUDA(cudaMemcpyAsync(h_label.data(), label.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  std::vector<std::vector<int32_t>> groups;
+  assemble_groups(n, h_label.data(), g->h_rp.data(), gmax, groups);
+  for (size_t gi = 0; gi < groups.size(); gi++)
+    for (int32_t v : groups[gi]) group_of_vertex[v] = (int32_t)gi;
+  *num_groups = (int32_t)groups.size();
+  if (iterations_run) *iterations_run = it;
+  label.release(); nlabel.release(); size.release(); join.release(); proposed.release(); rows.release();
+  count.release(); prop.release(); gscratch.release(); changed.release();
+  return HSDL_OK;
+}
+
+}  // namespace hsdl

@@ -22,27 +22,42 @@ namespace hsdl {
 
 namespace {
 
-// Each warp answers its queries in grid-stride order; `ahead` > 0 makes lane
-// 0 prefetch the rows of the query `ahead` strides further on into L2.
+// Each group of G lanes answers one query; the warp takes 32/G queries per
+// step in grid-stride order.  `ahead` > 0 makes the warp prefetch the rows of
+// the queries `ahead` steps further on into L2.
+template <int G>
 __global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
                         const int32_t* __restrict__ qk, const int64_t* __restrict__ off,
                         const uint32_t* __restrict__ hub, const uint32_t* __restrict__ hd, int32_t* __restrict__ out,
                         int ahead) {
-  const int lane = lane_id();
-  const int64_t step = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (ahead > 0 && lane < ahead) {
-    int64_t p = q + lane * step;
-    if (p < nq) prefetch_rows(off, hub, n, qs[p], qt[p]);
-  }
-  for (; q < nq; q += step) {
-    if (ahead > 0 && lane == 0) {
-      int64_t p = q + ahead * step;
+  constexpr int Q = 32 / G;  // queries per warp step
+  const int lane = lane_id(), grp = lane / G, gl = lane & (G - 1);
+  const int64_t step = (((int64_t)gridDim.x * blockDim.x) >> 5) * Q;
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * Q; base < nq; base += step) {
+    if (ahead > 0 && gl == 0) {
+      const int64_t p = base + (int64_t)ahead * step + grp;
       if (p < nq) prefetch_rows(off, hub, n, qs[p], qt[p]);
     }
-    const int32_t ans = warp_query(n, off, hub, hd, qs[q], qt[q], qk[q]);
-    if (lane == 0) out[q] = ans;
+    const int64_t q = base + grp;
+    const bool active = q < nq;
+    const int s = active ? qs[q] : 0, t = active ? qt[q] : 0, k = active ? qk[q] : 0;
+    const int32_t ans = group_query<G>(active, n, off, hub, hd, s, t, k);
+    if (active && gl == 0) out[q] = ans;
   }
+}
+
+template <int G>
+int launch_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k, int32_t* out,
+                 cudaStream_t st) {
+  const int sms = device_sm_count();
+  const int threads = idx->q_threads;
+  const int64_t warps = (nq + (32 / G) - 1) / (32 / G);
+  int64_t blocks = (warps * 32 + threads - 1) / threads;
+  int64_t max_blocks = (int64_t)sms * resident_blocks(k_query<G>, threads);
+  k_query<G><<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p,
+                                                                          idx->hub.p, idx->hd.p, out, idx->q_ahead);
+  HSDL_LAUNCHED();
+  return HSDL_OK;
 }
 
 }  // namespace
@@ -50,14 +65,14 @@ __global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, c
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st) {
   if (nq <= 0) return HSDL_OK;
-  const int sms = device_sm_count();
-  const int threads = idx->q_threads;
-  int64_t blocks = (nq * 32 + threads - 1) / threads;
-  int64_t max_blocks = (int64_t)sms * resident_blocks(k_query, threads);
-  k_query<<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p, idx->hub.p,
-                                                                       idx->hd.p, out, idx->q_ahead);
-  HSDL_LAUNCHED();
-  return HSDL_OK;
+  switch (idx->q_lanes) {
+    case 8:
+      return launch_query<8>(idx, nq, s, t, k, out, st);
+    case 16:
+      return launch_query<16>(idx, nq, s, t, k, out, st);
+    default:
+      return launch_query<32>(idx, nq, s, t, k, out, st);
+  }
 }
 
 int query_error(hsdl_index_impl* idx) {

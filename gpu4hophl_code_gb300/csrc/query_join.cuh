@@ -22,15 +22,17 @@
 namespace hsdl {
 
 // One lane's share of the merge-path join of hub rows A (la labels) and B (lb
-// labels) under hop bound k >= 1; returns the lane's minimum (INT_MAX if none).
-// A and B may point to shared or global memory; Ahd/Bhd are the matching
-// hop|distance words in global memory (read only on hub matches).
+// labels) under hop bound k >= 1, the merge split over a group of G lanes
+// (G = 8, 16 or 32; gl = lane index in the group); returns the lane's minimum
+// (INT_MAX if none).  A and B may point to shared or global memory; Ahd/Bhd
+// are the matching hop|distance words (read only on hub matches).
+template <int G>
 __device__ inline long long lane_merge(const uint32_t* A, int la, const uint32_t* B, int lb,
-                                       const uint32_t* __restrict__ Ahd, const uint32_t* __restrict__ Bhd, int k) {
-  const int lane = lane_id();
+                                       const uint32_t* __restrict__ Ahd, const uint32_t* __restrict__ Bhd, int k,
+                                       int gl) {
   long long best = INT_MAX;
   const int tot = la + lb;
-  const int d0 = (int)(((int64_t)tot * lane) >> 5), d1 = (int)(((int64_t)tot * (lane + 1)) >> 5);
+  const int d0 = (int)(((int64_t)tot * gl) / G), d1 = (int)(((int64_t)tot * (gl + 1)) / G);
   if (d0 < d1) {
     // merge-path split of diagonal d0: ia labels of A precede it
     int lo = max(0, d0 - lb), hi = min(d0, la);
@@ -65,6 +67,17 @@ __device__ inline long long lane_merge(const uint32_t* A, int la, const uint32_t
     }
   }
   return best;
+}
+
+// Min over the G lanes of each group (every lane of the warp must call it).
+template <int G>
+__device__ inline long long group_min(long long v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  return v;
 }
 
 // TMA bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, multiple of 16).
@@ -109,18 +122,33 @@ __device__ inline bool trivial_answer(int32_t n, int s, int t, int k, int32_t* a
 
 __device__ inline int32_t clamp_answer(long long best) { return best >= INT_MAX ? INT_MAX : (int32_t)best; }
 
-// The whole answer of (s, t, k) with both rows read from global memory.
+// Each group of G lanes answers its own (s, t, k), rows read from global
+// memory; every lane of the warp must call it (inactive groups pass
+// active = false).  Every lane of a group returns the group's answer.
+template <int G>
+__device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __restrict__ off,
+                                      const uint32_t* __restrict__ hub, const uint32_t* __restrict__ hd, int s,
+                                      int t, int k) {
+  int32_t ans = INT_MAX;
+  long long best = INT_MAX;
+  const bool trivial = !active || trivial_answer(n, s, t, k, &ans);
+  if (!trivial) {
+    int64_t a0 = off[s], a1 = off[s + 1], b0 = off[t], b1 = off[t + 1];
+    if (a1 - a0 > b1 - b0) {  // A = the shorter row
+      int64_t x = a0; a0 = b0; b0 = x;
+      x = a1; a1 = b1; b1 = x;
+    }
+    best = lane_merge<G>(hub + a0, (int)(a1 - a0), hub + b0, (int)(b1 - b0), hd + a0, hd + b0, k,
+                         lane_id() & (G - 1));
+  }
+  best = group_min<G>(best);
+  return trivial ? ans : clamp_answer(best);
+}
+
+// The whole answer of one (s, t, k) by a full warp (every lane must call it).
 __device__ inline int32_t warp_query(int32_t n, const int64_t* __restrict__ off, const uint32_t* __restrict__ hub,
                                      const uint32_t* __restrict__ hd, const int s, const int t, const int k) {
-  int32_t ans;
-  if (trivial_answer(n, s, t, k, &ans)) return ans;
-  int64_t a0 = off[s], a1 = off[s + 1], b0 = off[t], b1 = off[t + 1];
-  if (a1 - a0 > b1 - b0) {  // A = the shorter row
-    int64_t x = a0; a0 = b0; b0 = x;
-    x = a1; a1 = b1; b1 = x;
-  }
-  long long best = lane_merge(hub + a0, (int)(a1 - a0), hub + b0, (int)(b1 - b0), hd + a0, hd + b0, k);
-  return clamp_answer(warp_min_ll(best));
+  return group_query<32>(true, n, off, hub, hd, s, t, k);
 }
 
 }  // namespace hsdl

@@ -119,10 +119,12 @@ __device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
 // coalesced store.  A worker answers all of its published tickets (up to 32
 // at once: their requests are read in parallel and their rows prefetched),
 // one after another.
+template <int G>
 __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
                                                unsigned long long* comp, unsigned long long mask,
                                                const IndexDesc* descs, int32_t max_idx, long long idle_ns,
                                                unsigned long long base) {
+  constexpr int Q = 32 / G;  // requests answered at once by one warp
   const int lane = lane_id();
   const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (gw == 0) {
@@ -149,6 +151,7 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
   }
   const unsigned long long W = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
   const unsigned long long w = (unsigned long long)(gw - 1);
+  const int grp = lane / G;
   unsigned long long done = 0;  // tickets of this worker answered so far
   unsigned int backoff = 64;
   for (;;) {
@@ -173,25 +176,27 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hd);
         d.n = __ldcg(&descs[r.x].n);
         d.valid = __ldcg(&descs[r.x].valid);
-        if (d.valid && cnt > 1) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
+        if (d.valid && cnt > Q) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
       }
+      if (lane < cnt && !d.valid) atomicAdd(&ctl->bad, 1ull);
       int32_t mine = INT_MAX;
-      for (int j = 0; j < cnt; j++) {
+      for (int r0 = 0; r0 < cnt; r0 += Q) {
+        // group grp answers request j = r0 + grp, held by lane j
+        const int j = min(r0 + grp, 31);
+        const int jvalid = __shfl_sync(0xffffffffu, d.valid, j);  // every lane shuffles
+        const bool active = r0 + grp < cnt && jvalid != 0;
         const int s = __shfl_sync(0xffffffffu, r.y, j);
         const int t = __shfl_sync(0xffffffffu, r.z, j);
         const int k = __shfl_sync(0xffffffffu, r.w, j);
-        const int valid = __shfl_sync(0xffffffffu, d.valid, j);
-        int32_t ans = INT_MAX;
-        if (valid) {
-          const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
-          const uint32_t* hb = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hub, j);
-          const uint32_t* hx = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hd, j);
-          const int n = __shfl_sync(0xffffffffu, d.n, j);
-          ans = warp_query(n, off, hb, hx, s, t, k);
-        } else if (lane == 0) {
-          atomicAdd(&ctl->bad, 1ull);
-        }
-        if (lane == j) mine = ans;
+        const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
+        const uint32_t* hb = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hub, j);
+        const uint32_t* hx = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hd, j);
+        const int n = __shfl_sync(0xffffffffu, d.n, j);
+        const int32_t ans = group_query<G>(active, n, off, hb, hx, s, t, k);
+        // lane j takes the answer of the group that served it
+        const int src = (lane >= r0 && lane < r0 + Q) ? (lane - r0) * G : 0;
+        const int32_t got = __shfl_sync(0xffffffffu, ans, src);
+        if (lane >= r0 && lane < r0 + Q) mine = got;
       }
       // one 8-byte store per answer carries its ticket, so the host needs no
       // ordering between slots
@@ -281,8 +286,15 @@ int launch_if_needed(ServerImpl* S) {
   HSDL_CUDA(cudaMemsetAsync(&S->ctl.p->exit_reason, 0, sizeof(unsigned int), S->stream));
   HSDL_CUDA(cudaStreamSynchronize(S->stream));
   long long idle_ns = (long long)(S->opts.idle_exit_s * 1e9);
-  k_serve<<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
-                                               S->descs.p, S->opts.max_indexes, idle_ns, processed);
+  if (S->opts.lanes_per_query == 8)
+    k_serve<8><<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
+                                                    S->descs.p, S->opts.max_indexes, idle_ns, processed);
+  else if (S->opts.lanes_per_query == 16)
+    k_serve<16><<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
+                                                     S->descs.p, S->opts.max_indexes, idle_ns, processed);
+  else
+    k_serve<32><<<S->opts.ctas, 256, 0, S->stream>>>(S->ctl.p, S->hctl_dev, S->ring_dev, S->comp_dev, S->mask,
+                                                     S->descs.p, S->opts.max_indexes, idle_ns, processed);
   HSDL_LAUNCHED();
   S->running = true;
   return HSDL_OK;
@@ -416,6 +428,7 @@ void hsdl_serve_opts_default(hsdl_serve_opts* o) {
   o->max_indexes = 1024;
   o->budget_bytes = (int64_t)120 << 30;
   o->idle_exit_s = 0.5;
+  o->lanes_per_query = 8;
 }
 
 int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
@@ -429,6 +442,8 @@ int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
   SRV_ARG(o.ring_log2 >= 10 && o.ring_log2 <= 26, "ring_log2 must be in [10, 26]");
   SRV_ARG(o.max_indexes >= 1 && o.max_indexes <= (1 << 20), "max_indexes out of range");
   SRV_ARG(o.idle_exit_s > 0 && o.idle_exit_s <= 60, "idle_exit_s must be in (0, 60]");
+  SRV_ARG(o.lanes_per_query == 8 || o.lanes_per_query == 16 || o.lanes_per_query == 32,
+          "lanes_per_query must be 8, 16 or 32");
   auto* S = new hsdl_server();
   S->opts = o;
   S->sms = device_sm_count();
@@ -698,6 +713,7 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
   });
   int64_t last_done = 0;
   int64_t idle_check = 0;
+  int64_t ready_first = 0;
   for (int64_t i = 0; i < n; i++) {
     uint64_t tk = base + (uint64_t)i;
     unsigned long long* slot = S->comp + (tk & S->mask);
@@ -706,15 +722,18 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
       // several line fetches in flight instead of one miss at a time
       for (int a = 1; a <= 16; a++) __builtin_prefetch(S->comp + ((tk + 8ull * (uint64_t)(8 + a)) & S->mask), 0, 0);
     }
+    bool first_look = true;
     for (;;) {
       unsigned long long v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
       if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) {
+        ready_first += first_look;
         int64_t now = mono_ns() - t_start;
         lat_ns[i] = (int32_t)std::min<int64_t>(INT32_MAX, now - arrive[i]);
         if (o->answers) o->answers[i] = (int32_t)(uint32_t)v;
         last_done = now;
         break;
       }
+      first_look = false;
       if (++idle_check > (1 << 20)) {
         idle_check = 0;
         if (cudaStreamQuery(S->stream) != cudaErrorNotReady) {
@@ -745,6 +764,7 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
   res->p99_us = pct(0.99) / 1e3;
   res->p999_us = pct(0.999) / 1e3;
   res->max_us = sorted.back() / 1e3;
+  res->ready_frac = (double)ready_first / (double)n;
   return HSDL_OK;
 }
 

@@ -147,6 +147,27 @@ class Graph:
             pass
 
 
+def group_lp(graph: Graph, max_group: int = 1024, max_iterations: int = 100):
+    """generate_Group_CDLP (Hybrid_Generation_Clean/include/vgroup/CDLP_group.cuh:20):
+    returns (group_of_vertex int32[n], number of groups, iterations run)."""
+    gov = np.zeros(graph.n, np.int32)
+    ng = C.c_int32()
+    it = C.c_int32()
+    check(lib().hsdl_group_lp(graph.handle, max_group, max_iterations, _ptr(gov), C.byref(ng), C.byref(it)))
+    return gov, ng.value, it.value
+
+
+def generate_Group_CDLP(instance_graph, groups: list, MAX_GROUP_SIZE: int, max_iterations: int = 100) -> None:
+    """Reference-shaped form: fills `groups` with one list of vertex ids per
+    group, groups ordered by total degree (largest first)."""
+    g = instance_graph if isinstance(instance_graph, Graph) else Graph(instance_graph)
+    gov, ng, _ = group_lp(g, MAX_GROUP_SIZE, max_iterations)
+    order = np.argsort(gov, kind="stable")
+    bounds = np.searchsorted(gov[order], np.arange(ng + 1))
+    groups.clear()
+    groups.extend(order[bounds[i]:bounds[i + 1]].tolist() for i in range(ng))
+
+
 def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block_threads: int = 0,
                frontier_tile: int = 0, prune_lanes: int = 0, device_budget_bytes: int = 0) -> N.hsdl_build_opts:
     o = N.hsdl_build_opts()
@@ -238,14 +259,15 @@ class Index:
         check(lib().hsdl_extract_path(self._h, s, t, k, _ptr(e), cap, C.byref(cnt)))
         return [tuple(x) for x in e[: cnt.value].tolist()]
 
-    def set_query_tuning(self, block_threads: int = 256, prefetch_ahead: int = 0) -> None:
-        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, 0)
+    def set_query_tuning(self, block_threads: int = 512, prefetch_ahead: int = 0, lanes_per_query: int = 32) -> None:
+        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, lanes_per_query)
         check(lib().hsdl_set_query_tuning(self._h, C.byref(t)))
 
     def query_tuning(self) -> dict:
         t = N.hsdl_query_tuning()
         check(lib().hsdl_get_query_tuning(self._h, C.byref(t)))
-        return {"block_threads": t.block_threads, "prefetch_ahead": t.prefetch_ahead}
+        return {"block_threads": t.block_threads, "prefetch_ahead": t.prefetch_ahead,
+                "lanes_per_query": t.lanes_per_query}
 
     def save(self, path: str) -> None:
         check(lib().hsdl_save_labels(self._h, path.encode()))
@@ -402,7 +424,7 @@ class Server:
     (hsdl_serve_* in include/hsdl.h)."""
 
     def __init__(self, ctas: int = 0, ring_log2: int = 22, max_indexes: int = 1024,
-                 budget_bytes: int = 120 << 30, idle_exit_s: float = 0.5):
+                 budget_bytes: int = 120 << 30, idle_exit_s: float = 0.5, lanes_per_query: int = 8):
         o = N.hsdl_serve_opts()
         lib().hsdl_serve_opts_default(C.byref(o))
         o.ctas = ctas
@@ -410,6 +432,7 @@ class Server:
         o.max_indexes = max_indexes
         o.budget_bytes = budget_bytes
         o.idle_exit_s = idle_exit_s
+        o.lanes_per_query = lanes_per_query
         self._h = C.c_void_p()
         check(lib().hsdl_serve_create(C.byref(o), C.byref(self._h)))
         self._keep = {}

@@ -91,6 +91,18 @@ int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, con
 int hsdl_graph_destroy(hsdl_graph* g);
 
 /* ------------------------------------------------------------------------
+ * Label-propagation grouping.  Replaces generate_Group_CDLP(graph, groups,
+ * G_max) (Hybrid_Generation_Clean/include/vgroup/CDLP_group.cuh:20) and its
+ * CDLP_GPU kernels (.../vgroup/CDLP/GPU_Community_Detection.cuh:29-213), in
+ * a deterministic form: capped label propagation (a label's joiners move only
+ * if they all fit under max_group), then the reference's greedy merge of small
+ * groups and ordering by total degree.  group_of_vertex[v] = index of v's
+ * group in that order; *num_groups = groups; *iterations = rounds run.
+ * ---------------------------------------------------------------------- */
+int hsdl_group_lp(hsdl_graph* g, int32_t max_group, int32_t max_iterations, int32_t* group_of_vertex,
+                  int32_t* num_groups, int32_t* iterations);
+
+/* ------------------------------------------------------------------------
  * Label generation.  Replaces hop_constrained_two_hop_labels_generation
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:513)
  * and the GPU label_gen (Hybrid_Generation_Clean/src/label_gen.cu:603).
@@ -158,13 +170,14 @@ int hsdl_query_batch_static(hsdl_index* idx, int64_t nq, const int32_t* s, const
                             int32_t* out);
 
 /* Launch parameters of the query kernel for one index (the autotuner's
- * knobs): threads per block (multiple of 32, 32..1024) and how many queries
- * ahead each warp prefetches rows into L2 (0..8). */
+ * knobs): threads per block (multiple of 32, 32..1024), how many queries
+ * ahead each warp prefetches rows into L2 (0..8), and lanes per query (8, 16
+ * or 32: a warp answers 32/lanes queries at once). */
 typedef struct hsdl_query_tuning {
   int32_t struct_size;
   int32_t block_threads;
   int32_t prefetch_ahead;
-  int32_t reserved;
+  int32_t lanes_per_query;
 } hsdl_query_tuning;
 int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* tuning);
 int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* tuning);
@@ -224,6 +237,8 @@ typedef struct hsdl_serve_opts {
   int32_t max_indexes;  /* graph slots */
   int64_t budget_bytes; /* admission budget for resident + pending label bytes */
   double idle_exit_s;   /* the loop returns after this long without requests */
+  int32_t lanes_per_query; /* 8, 16 or 32 lanes answer one request (default 8) */
+  int32_t reserved;
 } hsdl_serve_opts;
 
 typedef struct hsdl_loadgen_opts {
@@ -245,6 +260,7 @@ typedef struct hsdl_loadgen_result {
   double achieved_qps;
   double offered_qps;
   double p50_us, p90_us, p99_us, p999_us, max_us; /* arrival -> answer seen */
+  double ready_frac;   /* answers already present when the host first looked */
 } hsdl_loadgen_result;
 
 typedef struct hsdl_serve_counters {

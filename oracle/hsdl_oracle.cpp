@@ -38,6 +38,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <vector>
 
@@ -637,5 +638,114 @@ void orc_bf(int n, const int64_t* rp, const int32_t* col, const int32_t* w, int 
 }
 
 const char* orc_last_error() { return g_err; }
+
+}  // extern "C"
+
+namespace {
+
+struct OrcGroup {
+  int64_t id, size;
+  std::vector<int32_t> nodes;
+  bool operator<(const OrcGroup& b) const { return size == b.size ? id < b.id : size < b.size; }
+};
+
+}  // namespace
+
+extern "C" {
+
+// Deterministic capped label propagation + the reference's group assembly.
+//  Propagation (GPU_Community_Detection.cuh:29-91, made deterministic):
+//   size[c] = |{v : label v = c}|; every vertex takes the most frequent label
+//   among its neighbours that is its own or has size < gmax (ties: smaller
+//   label; no eligible neighbour label: keep its own); the vertices proposing
+//   label c != their own move iff size[c] + their number <= gmax; stop when
+//   nothing moves or after max_iter rounds.
+//  Assembly (CDLP_group.cuh:39-100): bucket by label in label order, drop
+//   empty buckets; repeatedly take the largest group (by (size, id)) and merge
+//   it with the largest other group that fits in gmax, else emit it; order the
+//   emitted groups by total degree, largest first.
+// group_of_vertex[v] = group index; returns the number of groups.
+int orc_lp_group(int n, const int64_t* rp, const int32_t* col, int gmax, int max_iter, int32_t* group_of_vertex,
+                 int32_t* iterations) {
+  std::vector<int32_t> label(n), size(n), join(n), prop(n), nl(n);
+  for (int v = 0; v < n; v++) label[v] = v;
+  std::vector<uint32_t> nb;
+  int it = 0;
+  for (; it < max_iter; it++) {
+    std::fill(size.begin(), size.end(), 0);
+    std::fill(join.begin(), join.end(), 0);
+    for (int v = 0; v < n; v++) size[label[v]]++;
+    for (int v = 0; v < n; v++) {
+      nb.clear();
+      for (int64_t e = rp[v]; e < rp[v + 1]; e++) nb.push_back((uint32_t)label[col[e]]);
+      std::sort(nb.begin(), nb.end());
+      int32_t best = label[v];
+      int64_t best_cnt = 0;
+      for (size_t i = 0; i < nb.size();) {
+        size_t j = i + 1;
+        while (j < nb.size() && nb[j] == nb[i]) j++;
+        int32_t c = (int32_t)nb[i];
+        if ((c == label[v] || size[c] < gmax) && (int64_t)(j - i) > best_cnt) {
+          best_cnt = (int64_t)(j - i);
+          best = c;
+        }
+        i = j;
+      }
+      prop[v] = best;
+      if (best != label[v]) join[best]++;
+    }
+    int64_t changed = 0;
+    for (int v = 0; v < n; v++) {
+      int32_t c = prop[v];
+      nl[v] = (c != label[v] && size[c] + join[c] <= gmax) ? c : label[v];
+      changed += nl[v] != label[v];
+    }
+    label.swap(nl);
+    if (changed == 0) {
+      it++;
+      break;
+    }
+  }
+  if (iterations) *iterations = it;
+  std::vector<std::vector<int32_t>> buckets(n), groups;
+  for (int v = 0; v < n; v++) buckets[label[v]].push_back(v);
+  for (auto& b : buckets)
+    if (!b.empty()) groups.push_back(b);
+  std::set<OrcGroup> se;
+  for (size_t g = 0; g < groups.size(); g++) se.insert(OrcGroup{(int64_t)g, (int64_t)groups[g].size(), groups[g]});
+  std::vector<std::vector<int32_t>> after;
+  while (!se.empty()) {
+    auto it1 = std::prev(se.end());
+    auto it2 = se.upper_bound(OrcGroup{(int64_t)groups.size(), gmax - it1->size, {}});
+    bool merged = false;
+    if (it2 != se.begin()) {
+      --it2;
+      if (it2 == it1) it2 = (it2 == se.begin()) ? se.end() : std::prev(it2);
+      if (it2 != se.end() && it2 != it1 && it1->size + it2->size <= gmax) {
+        OrcGroup a = *it1;
+        a.size += it2->size;
+        a.nodes.insert(a.nodes.end(), it2->nodes.begin(), it2->nodes.end());
+        se.erase(it1);
+        se.erase(it2);
+        se.insert(a);
+        merged = true;
+      }
+    }
+    if (!merged) {
+      after.push_back(it1->nodes);
+      se.erase(it1);
+    }
+  }
+  std::vector<OrcGroup> order;
+  for (size_t g = 0; g < after.size(); g++) {
+    int64_t tot = 0;
+    for (int32_t v : after[g]) tot -= rp[v + 1] - rp[v];
+    order.push_back(OrcGroup{(int64_t)g, tot, after[g]});
+  }
+  std::sort(order.begin(), order.end());
+  for (size_t g = 0; g < order.size(); g++)
+    for (int32_t v : order[g].nodes) group_of_vertex[v] = (int32_t)g;
+  return (int)order.size();
+}
 
 }  // extern "C"

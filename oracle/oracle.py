@@ -75,6 +75,8 @@ class Oracle:
         L.orc_path.argtypes = [vp, i32, i32, i32, vp, i32]
         L.orc_free.argtypes = [vp]
         L.orc_bf.argtypes = [i32, vp, vp, vp, i32, i32, vp]
+        L.orc_lp_group.restype = i32
+        L.orc_lp_group.argtypes = [i32, vp, vp, i32, i32, vp, vp]
         self.L = L
 
     # -- handles -------------------------------------------------------------
@@ -132,6 +134,14 @@ class Oracle:
         out = np.zeros(g.n, np.int32)
         self.L.orc_bf(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), src, k, _p(out))
         return out
+
+    def lp_group(self, g, max_group: int, max_iterations: int = 100):
+        """Deterministic capped label propagation + the reference's group
+        assembly; returns (group_of_vertex, number of groups, iterations)."""
+        gov = np.zeros(g.n, np.int32)
+        it = np.zeros(1, np.int32)
+        ng = self.L.orc_lp_group(g.n, _p(g.row_ptr), _p(g.col), max_group, max_iterations, _p(gov), _p(it))
+        return gov, int(ng), int(it[0])
 
 
 class Reference:
