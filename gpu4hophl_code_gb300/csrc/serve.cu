@@ -689,16 +689,31 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
     }
   }
   std::vector<int32_t> lat_ns((size_t)n);
-  std::atomic<uint64_t> consumed_mirror{S->consumed};
+  // Answers arrive in host memory over the host link; reading them one line
+  // (8 answers) at a time from a single thread serialises a link round trip
+  // per line.  Several consumer threads each own every R-th chunk of 64
+  // tickets, so their line fetches overlap.  The producer's flow control
+  // uses the slowest consumer's position.
+  const int R = std::max(1, std::min(8, o->consumers > 0 ? o->consumers : 4));
+  constexpr int64_t kChunk = 64;
+  std::vector<std::atomic<int64_t>> cons_next(R);  // next index (relative) each consumer waits for
+  for (int c = 0; c < R; c++) cons_next[c].store(c * kChunk);
+  auto min_consumed = [&]() -> uint64_t {
+    int64_t m = n;
+    for (int c = 0; c < R; c++) m = std::min(m, cons_next[c].load(std::memory_order_acquire));
+    return base + (uint64_t)m;
+  };
   std::atomic<int> failed{0};
-  int64_t t_start = mono_ns() + 2000000;  // 2 ms to let both threads start
+  std::atomic<int64_t> last_done_ns{0};
+  std::atomic<int64_t> ready_first{0};
+  int64_t t_start = mono_ns() + 2000000;  // 2 ms to let the threads start
   HSDL_TRY(launch_if_needed(S));
   std::thread producer([&] {
     int64_t i = 0;
-    while (i < n && !failed.load()) {
+    while (i < n && !failed.load(std::memory_order_relaxed)) {
       int64_t now = mono_ns() - t_start;
       if (now < arrive[i]) continue;
-      uint64_t room = S->cap - (S->tail - consumed_mirror.load(std::memory_order_acquire));
+      uint64_t room = S->cap - (S->tail - min_consumed());
       if (room == 0) continue;
       int64_t j = i;
       while (j < n && (uint64_t)(j - i) < room && arrive[j] <= now && j - i < 4096) {
@@ -711,47 +726,63 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
       i = j;
     }
   });
-  int64_t last_done = 0;
-  int64_t idle_check = 0;
-  int64_t ready_first = 0;
-  for (int64_t i = 0; i < n; i++) {
-    uint64_t tk = base + (uint64_t)i;
-    unsigned long long* slot = S->comp + (tk & S->mask);
-    if ((tk & 7) == 0) {
-      // completion lines are written by the GPU over the host link; keep
-      // several line fetches in flight instead of one miss at a time
-      for (int a = 1; a <= 16; a++) __builtin_prefetch(S->comp + ((tk + 8ull * (uint64_t)(8 + a)) & S->mask), 0, 0);
-    }
-    bool first_look = true;
-    for (;;) {
-      unsigned long long v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
-      if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) {
-        ready_first += first_look;
-        int64_t now = mono_ns() - t_start;
-        lat_ns[i] = (int32_t)std::min<int64_t>(INT32_MAX, now - arrive[i]);
-        if (o->answers) o->answers[i] = (int32_t)(uint32_t)v;
-        last_done = now;
-        break;
-      }
-      first_look = false;
-      if (++idle_check > (1 << 20)) {
-        idle_check = 0;
-        if (cudaStreamQuery(S->stream) != cudaErrorNotReady) {
-          // the loop returned (idle or error): relaunch
-          S->running = true;
-          if (launch_if_needed(S) != HSDL_OK) {
-            failed = 1;
-            break;
+  auto consumer = [&](int c) {
+    int64_t ready = 0, latest = 0;
+    for (int64_t c0 = (int64_t)c * kChunk; c0 < n; c0 += (int64_t)R * kChunk) {
+      const int64_t c1 = std::min<int64_t>(n, c0 + kChunk);
+      for (int64_t i = c0; i < c1; i++) {
+        uint64_t tk = base + (uint64_t)i;
+        unsigned long long* slot = S->comp + (tk & S->mask);
+        bool first_look = true;
+        int64_t spins = 0;
+        unsigned long long v;
+        for (;;) {
+          v = __atomic_load_n(slot, __ATOMIC_ACQUIRE);
+          if ((uint32_t)(v >> 32) == (uint32_t)(tk + 1)) break;
+          first_look = false;
+          if (failed.load(std::memory_order_relaxed)) return;
+          if (++spins > (1 << 22)) {
+            spins = 0;
+            if (mono_ns() - t_start > (int64_t)120 * 1000000000) {
+              failed = 1;  // two minutes without this answer: give up
+              return;
+            }
           }
         }
+        ready += first_look;
+        if (i == c0 || (tk & 7) == 0) latest = mono_ns() - t_start;  // one clock read per line
+        lat_ns[i] = (int32_t)std::min<int64_t>(INT32_MAX, std::max<int64_t>(0, latest - arrive[i]));
+        if (o->answers) o->answers[i] = (int32_t)(uint32_t)v;
       }
+      cons_next[c].store(std::min<int64_t>(n, c0 + (int64_t)R * kChunk), std::memory_order_release);
     }
-    if (failed.load()) break;
-    S->consumed = tk + 1;
-    consumed_mirror.store(S->consumed, std::memory_order_release);
-  }
+    cons_next[c].store(n, std::memory_order_release);
+    ready_first.fetch_add(ready);
+    int64_t prev = last_done_ns.load();
+    while (latest > prev && !last_done_ns.compare_exchange_weak(prev, latest)) {
+    }
+  };
+  std::vector<std::thread> consumers;
+  for (int c = 1; c < R; c++) consumers.emplace_back(consumer, c);
+  // this thread consumes chunk 0 mod R and watches the loop
+  // relaunches the loop if it returned (it does so after idle_exit_s without
+  // new requests) while answers are still outstanding
+  std::thread watch([&] {
+    while (!failed.load() && min_consumed() < base + (uint64_t)n) {
+      std::this_thread::sleep_for(std::chrono::milliseconds(2));
+      if (cudaStreamQuery(S->stream) != cudaErrorNotReady && launch_if_needed(S) != HSDL_OK) failed = 1;
+    }
+  });
+  consumer(0);
+  for (auto& th : consumers) th.join();
+  watch.join();
+  int64_t last_done = last_done_ns.load();
+  S->consumed = base + (uint64_t)n;
   producer.join();
-  if (failed.load()) return HSDL_ERR_CUDA;
+  if (failed.load()) {
+    set_error("serving loop stopped answering during the load run");
+    return HSDL_ERR_TIMEOUT;
+  }
   std::vector<int32_t> sorted(lat_ns);
   std::sort(sorted.begin(), sorted.end());
   auto pct = [&](double p) { return sorted[std::min<size_t>(sorted.size() - 1, (size_t)(p * (sorted.size() - 1)))]; };
@@ -764,7 +795,7 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
   res->p99_us = pct(0.99) / 1e3;
   res->p999_us = pct(0.999) / 1e3;
   res->max_us = sorted.back() / 1e3;
-  res->ready_frac = (double)ready_first / (double)n;
+  res->ready_frac = (double)ready_first.load() / (double)n;
   return HSDL_OK;
 }
 

@@ -479,7 +479,8 @@ class Server:
             check(lib().hsdl_serve_wait(self._h, first.value, hi - lo, _ptr(out[lo:hi]), timeout_s))
         return out
 
-    def loadgen(self, g, s, t, k, offered_qps: float = 0.0, seed: int = 1, want_answers: bool = True) -> dict:
+    def loadgen(self, g, s, t, k, offered_qps: float = 0.0, seed: int = 1, want_answers: bool = True,
+                consumers: int = 4) -> dict:
         g = np.ascontiguousarray(g, np.int32)
         s = np.ascontiguousarray(s, np.int32)
         t = np.ascontiguousarray(t, np.int32)
@@ -492,6 +493,7 @@ class Server:
         o.answers = ans.ctypes.data if ans is not None else None
         o.offered_qps = offered_qps
         o.seed = seed
+        o.consumers = consumers
         r = N.hsdl_loadgen_result()
         check(lib().hsdl_serve_loadgen(self._h, C.byref(o), C.byref(r)))
         res = {f: getattr(r, f) for f, _ in N.hsdl_loadgen_result._fields_}

@@ -243,7 +243,7 @@ typedef struct hsdl_serve_opts {
 
 typedef struct hsdl_loadgen_opts {
   int32_t struct_size; /* sizeof(hsdl_loadgen_opts) */
-  int32_t reserved;
+  int32_t consumers;   /* host threads reading answers (0 = 4, at most 8) */
   int64_t n;           /* requests */
   const int32_t* g;    /* graph id, source, target, hop bound per request */
   const int32_t* s;
