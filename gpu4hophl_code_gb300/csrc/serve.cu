@@ -428,7 +428,7 @@ void hsdl_serve_opts_default(hsdl_serve_opts* o) {
   o->max_indexes = 1024;
   o->budget_bytes = (int64_t)120 << 30;
   o->idle_exit_s = 0.5;
-  o->lanes_per_query = 8;
+  o->lanes_per_query = 32;
 }
 
 int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {

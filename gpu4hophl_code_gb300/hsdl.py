@@ -424,7 +424,7 @@ class Server:
     (hsdl_serve_* in include/hsdl.h)."""
 
     def __init__(self, ctas: int = 0, ring_log2: int = 22, max_indexes: int = 1024,
-                 budget_bytes: int = 120 << 30, idle_exit_s: float = 0.5, lanes_per_query: int = 8):
+                 budget_bytes: int = 120 << 30, idle_exit_s: float = 0.5, lanes_per_query: int = 32):
         o = N.hsdl_serve_opts()
         lib().hsdl_serve_opts_default(C.byref(o))
         o.ctas = ctas

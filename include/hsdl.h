@@ -237,7 +237,7 @@ typedef struct hsdl_serve_opts {
   int32_t max_indexes;  /* graph slots */
   int64_t budget_bytes; /* admission budget for resident + pending label bytes */
   double idle_exit_s;   /* the loop returns after this long without requests */
-  int32_t lanes_per_query; /* 8, 16 or 32 lanes answer one request (default 8) */
+  int32_t lanes_per_query; /* 8, 16 or 32 lanes answer one request (default 32) */
   int32_t reserved;
 } hsdl_serve_opts;
 
