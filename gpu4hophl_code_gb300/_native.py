@@ -102,6 +102,7 @@ SIGNATURES = {
     "hsdl_build_opts_default": (None, [C.POINTER(hsdl_build_opts)]),
     "hsdl_wave_bounds": (C.c_int, [I32, C.POINTER(hsdl_build_opts), P, I32, C.POINTER(I32)]),
     "hsdl_build": (C.c_int, [P, I32, C.POINTER(hsdl_build_opts), PP]),
+    "hsdl_build_batched": (C.c_int, [I32, P, P, P, P, P, C.POINTER(hsdl_build_opts), P]),
     "hsdl_clean": (C.c_int, [P]),
     "hsdl_query_batch": (C.c_int, [P, I64, P, P, P, P]),
     "hsdl_query_batch_device": (C.c_int, [P, I64, P, P, P, P, P]),

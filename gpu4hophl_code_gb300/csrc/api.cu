@@ -170,6 +170,43 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
 
 }  // namespace
 
+namespace hsdl {
+
+int new_index_handle(hsdl_index** out) { return new_index(out); }
+void free_index_handle(hsdl_index* idx) { free_index(idx); }
+
+// Copies a (validated) host CSR into g's device buffers.
+int upload_graph(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w, hsdl_graph_impl* g) {
+  g->n = n;
+  g->m2 = row_ptr[n];
+  std::vector<int2> adj((size_t)g->m2);
+  int32_t mw = 0;
+  for (int64_t e = 0; e < g->m2; e++) {
+    adj[e] = make_int2(col[e], w[e]);
+    mw = std::max(mw, w[e]);
+  }
+  g->max_w = mw;
+  int rc = g->rp.alloc((int64_t)n + 1, nullptr);
+  if (rc == HSDL_OK) rc = g->adj.alloc(std::max<int64_t>(1, g->m2), nullptr);
+  if (rc == HSDL_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = HSDL_ERR_CUDA;
+  if (rc == HSDL_OK) {
+    cudaError_t e1 = cudaMemcpy(g->rp.p, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice);
+    cudaError_t e2 = g->m2 ? cudaMemcpy(g->adj.p, adj.data(), sizeof(int2) * g->m2, cudaMemcpyHostToDevice)
+                           : cudaSuccess;
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      set_error(std::string("graph upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+      rc = HSDL_ERR_CUDA;
+    }
+  }
+  if (rc != HSDL_OK) {
+    g->rp.release();
+    g->adj.release();
+  }
+  return rc;
+}
+
+}  // namespace hsdl
+
 extern "C" {
 
 const char* hsdl_last_error(void) { return last_error_cstr(); }
@@ -301,34 +338,12 @@ int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, con
   HSDL_CHECK_ARG(out, "null output");
   HSDL_TRY(hsdl_validate_csr(n, row_ptr, col, w));
   auto* g = new hsdl_graph();
-  g->n = n;
-  g->m2 = row_ptr[n];
-  g->h_rp.assign(row_ptr, row_ptr + n + 1);
-  std::vector<int2> adj((size_t)g->m2);
-  int32_t mw = 0;
-  for (int64_t e = 0; e < g->m2; e++) {
-    adj[e] = make_int2(col[e], w[e]);
-    mw = std::max(mw, w[e]);
-  }
-  g->max_w = mw;
-  int rc = g->rp.alloc((int64_t)n + 1, nullptr);
-  if (rc == HSDL_OK) rc = g->adj.alloc(std::max<int64_t>(1, g->m2), nullptr);
-  if (rc == HSDL_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = HSDL_ERR_CUDA;
-  if (rc == HSDL_OK) {
-    cudaError_t e1 = cudaMemcpy(g->rp.p, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice);
-    cudaError_t e2 = g->m2 ? cudaMemcpy(g->adj.p, adj.data(), sizeof(int2) * g->m2, cudaMemcpyHostToDevice)
-                           : cudaSuccess;
-    if (e1 != cudaSuccess || e2 != cudaSuccess) {
-      set_error(std::string("graph upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
-      rc = HSDL_ERR_CUDA;
-    }
-  }
+  int rc = upload_graph(n, row_ptr, col, w, g);
   if (rc != HSDL_OK) {
-    g->rp.release();
-    g->adj.release();
     delete g;
     return rc;
   }
+  g->h_rp.assign(row_ptr, row_ptr + n + 1);
   *out = g;
   return HSDL_OK;
 }

@@ -59,15 +59,30 @@ struct Counters {
   unsigned long long hop_f[16];   // frontier size of each hop
 };
 
+// Where slot rows live.  One graph: slot s owns cand[s*n .. s*n + n) and vertex
+// ids are row indices.  A batch of graphs laid out as one disjoint union: slot
+// s owns base[s] .. base[s] + (size of its hub's graph), a vertex's index in
+// the row is its id inside its own graph (lid), and each vertex carries its
+// graph's hop bound (vk).
+struct SlotMap {
+  int32_t n;
+  const int64_t* base;
+  const int32_t* lid;
+  const uint8_t* vk;
+  __device__ int64_t row(int slot) const { return base ? base[slot] : (int64_t)slot * n; }
+  __device__ int32_t local(int v) const { return lid ? lid[v] : v; }
+  __device__ int hop_bound(int hub, int K) const { return vk ? (int)vk[hub] : K; }
+};
+
 // ---------------------------------------------------------------------------
 // wave set-up
 // ---------------------------------------------------------------------------
-__global__ void k_wave_init(int32_t W, int32_t s_hub, int32_t n, uint64_t* __restrict__ cand, int2* __restrict__ C,
+__global__ void k_wave_init(int32_t W, int32_t s_hub, SlotMap map, uint64_t* __restrict__ cand, int2* __restrict__ C,
                             int4* __restrict__ F, Counters* ctr) {
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot < W) {
     int hub = s_hub + slot;
-    cand[(int64_t)slot * n + hub] = ckey(0, 0, (uint32_t)hub);
+    cand[map.row(slot) + map.local(hub)] = ckey(0, 0, (uint32_t)hub);
     C[slot] = make_int2(slot, hub);
     F[slot] = make_int4(slot, hub, 0, 0);
   }
@@ -159,7 +174,7 @@ __global__ void k_table_prefix(const Counters* ctr, int32_t* __restrict__ tab, i
 // sorted by neighbour id, so they are the suffix after the hub's id, found by
 // binary search.  The tile's relaxations are spread evenly over the block
 // through an exclusive scan of the suffix lengths.
-__global__ void __launch_bounds__(kThreads) k_expand(int32_t n, int32_t h, int32_t s_hub,
+__global__ void __launch_bounds__(kThreads) k_expand(SlotMap map, int32_t h, int32_t K, int32_t s_hub,
                                                      const int64_t* __restrict__ rp, const int2* __restrict__ adj,
                                                      const int4* __restrict__ F, uint64_t* __restrict__ cand,
                                                      int2* __restrict__ C, int64_t capC, Counters* ctr) {
@@ -172,7 +187,7 @@ __global__ void __launch_bounds__(kThreads) k_expand(int32_t n, int32_t h, int32
     int64_t i = tile * kThreads + threadIdx.x;
     int64_t len = 0, lo = 0;
     int4 e = make_int4(0, 0, 0, 0);
-    if (i < nf) {
+    if (i < nf && h <= map.hop_bound(s_hub + F[i].x, K)) {
       e = F[i];
       int hub = s_hub + e.x;
       lo = rp[e.y];
@@ -200,7 +215,7 @@ __global__ void __launch_bounds__(kThreads) k_expand(int32_t n, int32_t h, int32
       int4 oe = s_e[a];
       int2 nb = adj[s_lo[a] + (j - s_start[a])];
       uint64_t key = ckey((uint32_t)oe.z + (uint32_t)nb.y, (uint32_t)h, (uint32_t)oe.y);
-      uint64_t* p = cand + (int64_t)oe.x * n + nb.x;
+      uint64_t* p = cand + map.row(oe.x) + map.local(nb.x);
       bool app = false;
       if (key < __ldcg((const unsigned long long*)p)) {
         uint64_t old = atomicMin((unsigned long long*)p, (unsigned long long)key);
@@ -226,7 +241,7 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 // ---------------------------------------------------------------------------
 // hop round: pruning query (one warp per candidate)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_prune(int32_t n, int32_t h, int32_t K, int32_t s_hub,
+__global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K, int32_t s_hub,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
                                                     const int64_t* __restrict__ row_off,
                                                     const int32_t* __restrict__ row_len,
@@ -244,7 +259,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(int32_t n, int32_t h, int32_
   for (int64_t i = c0 + warp; i < c1; i += nwarps) {
     int2 e = C[i];
     int slot = e.x, v = e.y;
-    uint64_t ck = cand[(int64_t)slot * n + v];
+    uint64_t ck = cand[map.row(slot) + map.local(v)];
     long long d = (long long)ckey_dist(ck);
     long long q = LLONG_MAX;
     int cap = tab_cap[slot];
@@ -285,7 +300,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(int32_t n, int32_t h, int32_
       wl_v[p] = v;
       wl_key[p] = lkey((uint32_t)(s_hub + slot), (uint32_t)h, (uint32_t)d);
       wl_par[p] = (int32_t)ckey_parent(ck);
-      if (h < K) {
+      if (h < map.hop_bound(s_hub + slot, K)) {
         unsigned long long f = atomicAdd(&ctr->hop_f[h], 1ull);
         Fout[f] = make_int4(slot, v, (int)d, 0);
       }
@@ -373,13 +388,13 @@ __global__ void k_clear_cnt(const Counters* ctr, const int32_t* __restrict__ tou
     cnt[touched[i]] = 0;
 }
 
-__global__ void k_reset(const Counters* ctr, const int2* __restrict__ C, uint64_t* __restrict__ cand, int32_t n,
+__global__ void k_reset(const Counters* ctr, const int2* __restrict__ C, uint64_t* __restrict__ cand, SlotMap map,
                         int64_t capC) {
   int64_t total = (int64_t)ctr->c_count;
   if (total > capC) total = capC;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     int2 e = C[i];
-    cand[(int64_t)e.x * n + e.y] = kEmptyCand;
+    cand[map.row(e.x) + map.local(e.y)] = kEmptyCand;
   }
 }
 
@@ -470,7 +485,8 @@ int row_max(int32_t n, const int64_t* d_off, int64_t* out, cudaStream_t st) {
   return HSDL_OK;
 }
 
-int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx) {
+int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx,
+                const BatchPlan* plan) {
   const int32_t n = g->n;
   cudaStream_t st = idx->stream;
   const int sms = device_sm_count();
@@ -480,10 +496,32 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   size_t free_b = 0, total_b = 0;
   HSDL_CUDA(cudaMemGetInfo(&free_b, &total_b));
   int64_t budget = opts.device_budget_bytes > 0 ? opts.device_budget_bytes : (int64_t)free_b;
-  int32_t max_wave = opts.max_wave > 0 ? opts.max_wave : auto_max_wave(n, budget);
-  std::vector<int32_t> bounds = wave_schedule(n, opts.first_wave > 0 ? opts.first_wave : 1, max_wave);
+  std::vector<int32_t> bounds;
+  if (plan) {
+    bounds = plan->bounds;
+  } else {
+    int32_t max_wave = opts.max_wave > 0 ? opts.max_wave : auto_max_wave(n, budget);
+    bounds = wave_schedule(n, opts.first_wave > 0 ? opts.first_wave : 1, max_wave);
+  }
   int32_t Wmax = 0;
-  for (size_t i = 0; i + 1 < bounds.size(); i++) Wmax = std::max(Wmax, bounds[i + 1] - bounds[i]);
+  int64_t cand_entries = 0;  // largest wave's candidate rows
+  for (size_t i = 0; i + 1 < bounds.size(); i++) {
+    Wmax = std::max(Wmax, bounds[i + 1] - bounds[i]);
+    int64_t e = 0;
+    if (plan) {
+      for (int32_t v = bounds[i]; v < bounds[i + 1]; v++) e += plan->comp_n[v];
+    } else {
+      e = (int64_t)(bounds[i + 1] - bounds[i]) * n;
+    }
+    cand_entries = std::max(cand_entries, e);
+  }
+  std::vector<int64_t> h_base;
+  DevBuf<int64_t> d_base;
+  if (plan) {
+    h_base.resize(Wmax);
+    HSDL_TRY(d_base.alloc(Wmax, st));
+  }
+  SlotMap map{n, plan ? d_base.p : nullptr, plan ? plan->lid : nullptr, plan ? plan->vk : nullptr};
 
   // --- device state --------------------------------------------------------
   DevBuf<uint64_t> cand;
@@ -503,14 +541,14 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     cand.release(); row_off.release(); row_len.release(); row_cap.release(); cnt.release(); touched.release();
     pool_keys.release(); pool_par.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
-    pool_tail.release();
+    pool_tail.release(); d_base.release();
   };
   struct Guard {
     std::function<void()> f;
     ~Guard() { f(); }
   } guard{release_all};
 
-  HSDL_TRY(cand.alloc((int64_t)Wmax * n, st));
+  HSDL_TRY(cand.alloc(cand_entries, st));
   HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)cand.bytes(), st));
   HSDL_TRY(row_off.alloc(n, st));
   HSDL_TRY(row_len.alloc(n, st));
@@ -551,9 +589,20 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   const int g_prune = sms * resident_blocks(k_prune, kThreads);
   for (size_t wv = 0; wv + 1 < bounds.size(); wv++) {
     const int32_t s_hub = bounds[wv], W = bounds[wv + 1] - bounds[wv];
+    int64_t wave_entries = (int64_t)W * n;
+    if (plan) {
+      // each slot's row is as long as its hub's graph
+      int64_t acc = 0;
+      for (int32_t i = 0; i < W; i++) {
+        h_base[i] = acc;
+        acc += plan->comp_n[s_hub + i];
+      }
+      wave_entries = acc;
+      HSDL_CUDA(cudaMemcpyAsync(d_base.p, h_base.data(), sizeof(int64_t) * W, cudaMemcpyHostToDevice, st));
+    }
     for (int attempt = 0;; attempt++) {
       HSDL_CUDA(cudaMemsetAsync(ctr.p, 0, sizeof(Counters), st));
-      k_wave_init<<<(W + 255) / 256, 256, 0, st>>>(W, s_hub, n, cand.p, Cl.p, Fa.p, ctr.p);
+      k_wave_init<<<(W + 255) / 256, 256, 0, st>>>(W, s_hub, map, cand.p, Cl.p, Fa.p, ctr.p);
       HSDL_LAUNCHED();
       k_table_size<<<1, 1024, 0, st>>>(W, s_hub, row_len.p, tab_cap.p, tab_off.p, ctr.p);
       HSDL_LAUNCHED();
@@ -575,11 +624,11 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       for (int32_t h = 1; h <= K; h++) {
         int4* Fin = (h & 1) ? Fa.p : Fb.p;
         int4* Fout = (h & 1) ? Fb.p : Fa.p;
-        k_expand<<<g_expand, kThreads, 0, st>>>(n, h, s_hub, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+        k_expand<<<g_expand, kThreads, 0, st>>>(map, h, K, s_hub, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
         HSDL_LAUNCHED();
         k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
         HSDL_LAUNCHED();
-        k_prune<<<g_prune, kThreads, 0, st>>>(n, h, K, s_hub, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p,
+        k_prune<<<g_prune, kThreads, 0, st>>>(map, h, K, s_hub, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p,
                                               tab_off.p, tab_cap.p, tab.p, stride, Fout, wl_v.p, wl_key.p,
                                               wl_par.p, ctr.p);
         HSDL_LAUNCHED();
@@ -590,7 +639,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       // The candidate list overflowed: entries past its end were never
       // recorded, so clear this wave's slots wholesale and rerun the wave with
       // room for twice what was asked.
-      HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)W * n * sizeof(uint64_t), st));
+      HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)wave_entries * sizeof(uint64_t), st));
       capC = std::max<int64_t>(capC * 2, (int64_t)hc.c_count * 2);
       HSDL_TRY(alloc_lists(capC));
       if (attempt > 40) {
@@ -624,7 +673,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       k_clear_cnt<<<grid, 256, 0, st>>>(ctr.p, touched.p, cnt.p);
       HSDL_LAUNCHED();
     }
-    k_reset<<<grid, 256, 0, st>>>(ctr.p, Cl.p, cand.p, n, capC);
+    k_reset<<<grid, 256, 0, st>>>(ctr.p, Cl.p, cand.p, map, capC);
     HSDL_LAUNCHED();
     idx->waves++;
   }

@@ -130,8 +130,20 @@ int resident_blocks(K kernel, int threads, size_t smem = 0) {
 }
 int max_row_length(hsdl_index_impl* idx, int64_t* out);  // recomputes from h_off
 
+// A batch of graphs built as one disjoint union (see batched.cu): explicit wave
+// bounds over the union's ids, each vertex's id inside its own graph (lid,
+// device), its graph's hop bound (vk, device) and its graph's size (comp_n,
+// host).
+struct BatchPlan {
+  std::vector<int32_t> bounds;
+  std::vector<int64_t> comp_n;
+  const int32_t* lid = nullptr;
+  const uint8_t* vk = nullptr;
+};
+
 // kernels / stages implemented in the .cu files
-int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx);
+int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx,
+                const BatchPlan* plan = nullptr);
 int clean_index(hsdl_index_impl* idx);
 int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,
              int32_t* iterations_run);

@@ -205,6 +205,21 @@ class Index:
         return cls(h)
 
     @classmethod
+    def build_batched(cls, graphs, Ks, **opts) -> list:
+        """Indexes many host graphs together (hsdl_build_batched); one Index per graph."""
+        B = len(graphs)
+        n = np.array([g.n for g in graphs], np.int32)
+        K = np.array(Ks, np.int32)
+        rps = (C.c_void_p * B)(*[g.row_ptr.ctypes.data for g in graphs])
+        cols = (C.c_void_p * B)(*[g.col.ctypes.data for g in graphs])
+        ws = (C.c_void_p * B)(*[g.w.ctypes.data for g in graphs])
+        outs = (C.c_void_p * B)()
+        o = build_opts(**opts)
+        check(lib().hsdl_build_batched(B, _ptr(n), C.cast(rps, C.c_void_p), C.cast(cols, C.c_void_p),
+                                       C.cast(ws, C.c_void_p), _ptr(K), C.byref(o), C.cast(outs, C.c_void_p)))
+        return [cls(C.c_void_p(outs[i])) for i in range(B)]
+
+    @classmethod
     def import_labels(cls, n: int, K: int, offsets: np.ndarray, labels: np.ndarray) -> "Index":
         offsets = np.ascontiguousarray(offsets, np.int64)
         labels = np.ascontiguousarray(labels, np.int32).reshape(-1, 4)

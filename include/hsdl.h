@@ -130,6 +130,17 @@ typedef struct hsdl_index hsdl_index;
 
 int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index** out);
 
+/* Builds (and cleans) many graphs at once: graph i is the CSR (n[i],
+ * row_ptr[i], col[i], w[i]) with hop bound K[i]; out[i] receives its index,
+ * bit-identical to hsdl_build of that graph alone.  The graphs run as one
+ * disjoint union whose waves hold the same ranks of many graphs together;
+ * graphs are grouped into sub-batches whose estimated labels fit
+ * opts->device_budget_bytes (0 = half of free HBM).  No counterpart in the
+ * reference, which builds one graph per run. */
+int hsdl_build_batched(int32_t num_graphs, const int32_t* n, const int64_t* const* row_ptr,
+                       const int32_t* const* col, const int32_t* const* w, const int32_t* K,
+                       const hsdl_build_opts* opts, hsdl_index** out);
+
 /* ------------------------------------------------------------------------
  * Canonical repair.  Replaces hop_constrained_clean_L
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:422)
