@@ -126,6 +126,17 @@ def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
     return int(4 * rows.sum() + 48 * len(s))
 
 
+def build_algorithmic_bytes(info: dict) -> int:
+    """Bytes the build must move, from the work the device counted: per
+    relaxation an 8-byte adjacency entry and an 8-byte candidate key; per
+    committed label read by a pruning join an 8-byte key; per label generated
+    an 8-byte key and a 4-byte parent; per label read by the clean's joins a
+    4-byte hub id and a 4-byte hop|distance word; per final label a read and a
+    write of 12 bytes (sort and compaction)."""
+    return int(16 * info["work_relaxations"] + 8 * info["work_join_reads"] + 12 * info["work_labels_written"] +
+               8 * info["work_clean_reads"] + 24 * info["labels"])
+
+
 def cpu_query_baseline(off, lab, s, t, k, seconds, threads):
     """Reference query path (hop_constrained_extract_distance restated in
     oracle/) over a bounded sample of the batch, on `threads` host cores.
@@ -182,10 +193,15 @@ def run_ours(args, dist, rank, world, local):
     g = make_graph(args.n)
     dev = H.Graph(g)
     torch.cuda.synchronize()
+    # label-propagation grouping into groups of at most 1,024 vertices
+    t0 = time.perf_counter()
+    _, n_groups, lp_iters = H.group_lp(dev, 1024, 100)
+    lp_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     idx = H.Index.build(dev, args.K, clean=True)
     build_s = time.perf_counter() - t0
     info = idx.info()
+    build_bytes = build_algorithmic_bytes(info)
 
     s, t, k = make_queries(args.n, args.queries, args.K, seed=1000 + rank)
     stream = torch.cuda.Stream()
@@ -309,7 +325,13 @@ def run_ours(args, dist, rank, world, local):
             "build": {"seconds": round(build_s, 3), "generate_s": round(info["time_generate_s"], 3),
                       "sort_s": round(info["time_sort_s"], 3), "clean_s": round(info["time_clean_s"], 3),
                       "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
-                      "labels_per_s": round(info["labels"] / build_s, 1), "waves": info["waves"]},
+                      "labels_per_s": round(info["labels"] / build_s, 1), "waves": info["waves"],
+                      "lp_grouping_s": round(lp_s, 3), "lp_groups": n_groups, "lp_iterations": lp_iters,
+                      "roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": peak,
+                                   "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / peak, 4),
+                                   "algorithmic_bytes": build_bytes,
+                                   "work": {k: info[k] for k in ("work_relaxations", "work_join_reads",
+                                                                 "work_labels_written", "work_clean_reads")}}},
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,

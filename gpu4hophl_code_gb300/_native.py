@@ -45,7 +45,8 @@ class hsdl_index_info(C.Structure):
     _fields_ = [("n", C.c_int32), ("K", C.c_int32), ("cleaned", C.c_int32), ("waves", C.c_int32),
                 ("labels", C.c_int64), ("labels_before_clean", C.c_int64), ("labels_after_clean", C.c_int64),
                 ("device_bytes", C.c_int64), ("time_generate_s", C.c_double), ("time_sort_s", C.c_double),
-                ("time_clean_s", C.c_double), ("max_row", C.c_int64)]
+                ("time_clean_s", C.c_double), ("max_row", C.c_int64), ("work_relaxations", C.c_int64),
+                ("work_join_reads", C.c_int64), ("work_labels_written", C.c_int64), ("work_clean_reads", C.c_int64)]
 
 
 class hsdl_serve_opts(C.Structure):

@@ -548,6 +548,10 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->time_sort_s = idx->t_sort;
   info->time_clean_s = idx->t_clean;
   info->max_row = idx->max_row;
+  info->work_relaxations = idx->work_relax;
+  info->work_join_reads = idx->work_join_reads;
+  info->work_labels_written = idx->work_labels_written;
+  info->work_clean_reads = idx->work_clean_reads;
   return HSDL_OK;
 }
 

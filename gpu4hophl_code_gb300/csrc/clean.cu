@@ -51,20 +51,25 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
                                                          const uint32_t* __restrict__ hd,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
                                                          int stride, int smem_slots, int32_t* __restrict__ gscratch,
-                                                         int64_t gscratch_slots, int* __restrict__ next_v) {
+                                                         int64_t gscratch_slots, int* __restrict__ next_v,
+                                                         unsigned long long* __restrict__ reads) {
   extern __shared__ int32_t smem_tab[];
   __shared__ int s_v;
   __shared__ int s_kept[kCleanThreads / 32];
   const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned long long scanned = 0;
   for (;;) {
     if (threadIdx.x == 0) s_v = atomicAdd(next_v, 1);
     __syncthreads();
     const int v = s_v;
-    if (v >= n) break;
+    if (v >= n) {
+      if (lane == 0 && scanned) atomicAdd(reads, scanned);
+      break;
+    }
     const int64_t lo = off[v];
     const int len = (int)(off[v + 1] - lo);
     int64_t cap = 8;
-    while (cap < 2 * (int64_t)len) cap <<= 1;
+    while (cap < (int64_t)len + len / 2) cap <<= 1;  // load factor <= 2/3
     int32_t* T = (cap <= smem_slots) ? smem_tab : gscratch + (int64_t)blockIdx.x * gscratch_slots * stride;
     const uint32_t mask = (uint32_t)cap - 1;
     for (int64_t i = threadIdx.x; i < cap * stride; i += blockDim.x) T[i] = kInf32;
@@ -115,11 +120,11 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
           for (int j0 = 0; j0 < ulen; j0 += 32) {
             int j = j0 + lane;
             if (j < ulen) {
-              int w = (int)hub[ulo + j];
+              const int w = (int)hub[ulo + j];
+              const uint32_t x1 = hd[ulo + j];  // issued with the hub id: no dependent load
               if (w != u) {
                 const int32_t* rw = tab_find(T, mask, stride, w);
-                if (rw) {  // hop and distance are read only for hubs v shares
-                  uint32_t x1 = hd[ulo + j];
+                if (rw) {
                   int h1 = (int)hd_hop(x1);
                   if (h1 <= h) {
                     int32_t t = rw[1 + h - h1];
@@ -131,6 +136,7 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
                 }
               }
             }
+            scanned += (unsigned long long)min(32, ulen - j0);
             if (__any_sync(0xffffffffu, q <= d)) break;
           }
           q = warp_min_ll(q);
@@ -187,12 +193,12 @@ int clean_index(hsdl_index_impl* idx) {
   const int sms = device_sm_count();
   const int stride = (K + 2 <= 8) ? 8 : 16;
   double t0 = now_s();
-  // shared-memory table: up to 96 KB per block
-  const int smem_slots = (96 * 1024) / (stride * 4);
+  // shared-memory table: 64 KB per block (three blocks per SM)
+  const int smem_slots = (64 * 1024) / (stride * 4);
   const size_t smem = (size_t)smem_slots * stride * 4;
   HSDL_CUDA(cudaFuncSetAttribute(k_clean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t need_slots = 8;
-  while (need_slots < 2 * idx->max_row) need_slots <<= 1;
+  while (need_slots < idx->max_row + idx->max_row / 2) need_slots <<= 1;
   const int grid = sms * resident_blocks(k_clean, kCleanThreads, smem);
   int64_t gslots = need_slots > smem_slots ? need_slots : 0;
   DevBuf<int32_t> gscratch;
@@ -200,17 +206,22 @@ int clean_index(hsdl_index_impl* idx) {
   DevBuf<uint8_t> keep;
   DevBuf<int64_t> kept, noff;
   DevBuf<int> next;
+  DevBuf<unsigned long long> reads;
+  HSDL_TRY(reads.alloc(1, st));
+  HSDL_CUDA(cudaMemsetAsync(reads.p, 0, sizeof(unsigned long long), st));
   HSDL_TRY(keep.alloc(std::max<int64_t>(1, idx->total), st));
   HSDL_TRY(kept.alloc((int64_t)n + 1, st));
   HSDL_TRY(noff.alloc((int64_t)n + 1, st));
   HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
   k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p, stride,
-                                             smem_slots, gscratch.p, gslots, next.p);
+                                             smem_slots, gscratch.p, gslots, next.p, reads.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
   int64_t total = 0;
+  unsigned long long h_reads = 0;
   HSDL_CUDA(cudaMemcpyAsync(&total, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  HSDL_CUDA(cudaMemcpyAsync(&h_reads, reads.p, sizeof(h_reads), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
   DevBuf<uint32_t> nhub, nhd;
   DevBuf<int32_t> npar;
@@ -237,6 +248,8 @@ int clean_index(hsdl_index_impl* idx) {
   kept.release();
   gscratch.release();
   next.release();
+  reads.release();
+  idx->work_clean_reads += (int64_t)h_reads;
   idx->before = idx->total;
   idx->total = total;
   idx->after = total;

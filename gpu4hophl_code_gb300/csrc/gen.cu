@@ -54,7 +54,8 @@ struct Counters {
   unsigned long long tab_total;   // hub-table slots this wave
   unsigned long long reloc_need;  // pool entries the commit's row moves need
   unsigned long long touched;     // rows receiving labels this wave
-  unsigned long long pad[2];
+  unsigned long long relax;       // relaxations this wave (work counter)
+  unsigned long long reads;       // committed labels read by the pruning join (work counter)
   unsigned long long hop_c[16];   // candidate-list start of each hop
   unsigned long long hop_f[16];   // frontier size of each hop
 };
@@ -202,6 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_expand(SlotMap map, int32_t h, int
     }
     int64_t total;
     int64_t pre = block_exclusive_scan(len, s_scan, &total);
+    if (threadIdx.x == 0 && total) atomicAdd(&ctr->relax, (unsigned long long)total);
     s_start[threadIdx.x] = pre;
     s_lo[threadIdx.x] = lo;
     s_e[threadIdx.x] = e;
@@ -256,6 +258,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
   const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned long long scanned = 0;
   for (int64_t i = c0 + warp; i < c1; i += nwarps) {
     int2 e = C[i];
     int slot = e.x, v = e.y;
@@ -291,6 +294,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
             }
           }
         }
+        scanned += (unsigned long long)min(32, len - j0);
         if (__any_sync(0xffffffffu, q <= d)) break;  // already dominated
       }
       q = warp_min_ll(q);
@@ -306,6 +310,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
       }
     }
   }
+  if (lane == 0 && scanned) atomicAdd(&ctr->reads, scanned);
 }
 
 // ---------------------------------------------------------------------------
@@ -647,6 +652,9 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
         return HSDL_ERR_NOMEM;
       }
     }
+    idx->work_relax += (int64_t)hc.relax;
+    idx->work_join_reads += (int64_t)hc.reads;
+    idx->work_labels_written += (int64_t)hc.wl_count;
     // commit the wave's labels
     if (hc.wl_count > 0) {
       k_count<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, cnt.p, touched.p, ctr.p);

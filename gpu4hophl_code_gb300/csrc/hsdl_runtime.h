@@ -114,6 +114,8 @@ struct hsdl_index_impl {
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;
   double t_gen = 0, t_sort = 0, t_clean = 0;
+  // work counted on the device during the build (for the roofline)
+  int64_t work_relax = 0, work_join_reads = 0, work_labels_written = 0, work_clean_reads = 0;
   cudaStream_t stream = nullptr;
   std::vector<int64_t> h_off;  // host copy of offsets (path extraction, export)
 };

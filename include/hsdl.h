@@ -215,6 +215,11 @@ typedef struct hsdl_index_info {
   double time_sort_s;            /* time_sortL */
   double time_clean_s;           /* time_canonical_repair */
   int64_t max_row;               /* longest label list */
+  /* work counted on the device during the build */
+  int64_t work_relaxations;      /* edges relaxed by the searches */
+  int64_t work_join_reads;       /* committed labels read by the pruning joins */
+  int64_t work_labels_written;   /* labels generated (before clean) */
+  int64_t work_clean_reads;      /* labels read by the clean's joins */
 } hsdl_index_info;
 
 int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);
