@@ -55,6 +55,10 @@ def parse():
                     help="offered Poisson rates (q/s) for the serving loop; 0 = as fast as the ring allows")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--workload", choices=["plain", "batched", "stress"], default="plain",
+                    help="batched: many small graphs built together; stress: the 4M-vertex graph with Zipf "
+                         "queries (each prints its own line)")
+    ap.add_argument("--graphs", type=int, default=4096, help="batched workload: number of graphs")
     return ap.parse_args()
 
 
@@ -326,6 +330,8 @@ def run_ours(args, dist, rank, world, local):
                       "sort_s": round(info["time_sort_s"], 3), "clean_s": round(info["time_clean_s"], 3),
                       "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
                       "labels_per_s": round(info["labels"] / build_s, 1), "waves": info["waves"],
+                      "peak_bytes": info["build_peak_bytes"], "pool_entries": info["build_pool_entries"],
+                      "max_wave_candidates": info["build_max_candidates"],
                       "lp_grouping_s": round(lp_s, 3), "lp_groups": n_groups, "lp_iterations": lp_iters,
                       "roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": peak,
                                    "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / peak, 4),
@@ -387,9 +393,176 @@ def run_reference(args, dist, rank, world, local):
             "e2e": {"value": round(v, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def make_batch(count, seed):
+    """Graphs of the batched workload: n log-uniform in [200, 50000], even
+    indexes Erdos-Renyi (average degree 6), odd Barabasi-Albert (m0 = 3),
+    weights uniform [1, 1000], K uniform in {3, 4, 5, 6}."""
+    import gpu4hophl_code_gb300 as H
+
+    rng = np.random.default_rng(seed)
+    graphs, Ks = [], []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(200), np.log(50000))))
+        if i % 2 == 0:
+            g = H.HostGraph.erdos_renyi(n, 3 * n, 1, 1000, seed=seed * 100003 + i)
+        else:
+            g = H.HostGraph.barabasi_albert(n, 3, 1, 1000, seed=seed * 100003 + i)
+        graphs.append(g)
+        Ks.append(int(rng.integers(3, 7)))
+    return graphs, Ks
+
+
+def run_batched(args, dist, rank, world, local):
+    """One step = hsdl_build_batched of the whole batch (generation + clean of
+    every graph, per-graph indexes out).  Launch shapes come from
+    hsdl_build_batched_autotune on 256 graphs spread over the batch (timed
+    separately).  A sample of graphs is checked bit-exact against their own
+    single builds."""
+    import torch
+
+    torch.cuda.set_device(local)
+    import gpu4hophl_code_gb300 as H
+
+    t0 = time.perf_counter()
+    graphs, Ks = make_batch(args.graphs, SEED + 7 + rank)
+    gen_s = time.perf_counter() - t0
+    total_n = int(sum(g.n for g in graphs))
+    total_m = int(sum(g.num_edges for g in graphs))
+    t0 = time.perf_counter()
+    tuned = H.autotune_build_batched(graphs, Ks, sample_graphs=256)
+    tune_s = time.perf_counter() - t0
+    shapes = {k: tuned[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    for _ in range(args.warmup):
+        for ix in H.Index.build_batched(graphs[:64], Ks[:64], **shapes):
+            ix.close()
+    times, labels = [], 0
+    for step in range(args.steps):
+        barrier(dist)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        idxs = H.Index.build_batched(graphs, Ks, **shapes)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        if step == args.steps - 1:
+            labels = int(sum(ix.info()["labels"] for ix in idxs))
+            rng = np.random.default_rng(5)
+            for i in rng.choice(len(graphs), size=min(16, len(graphs)), replace=False):
+                dev = H.Graph(graphs[i])
+                single = H.Index.build(dev, Ks[i]).export()
+                got = idxs[i].export()
+                assert np.array_equal(got[0], single[0]) and np.array_equal(got[1], single[1]), i
+        for ix in idxs:
+            ix.close()
+    t0 = time.perf_counter()
+    default = H.Index.build_batched(graphs, Ks)
+    default_s = time.perf_counter() - t0
+    for ix in default:
+        ix.close()
+    best = max_over_ranks(dist, float(np.median(times)))
+    if rank != 0:
+        return None
+    return {
+        "metric": "batched build graphs/s (generation + clean, per-graph canonical labels)",
+        "value": round(args.graphs * world / best, 1), "unit": "graphs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(best * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded Erdos-Renyi and Barabasi-Albert graphs)",
+        "config": {"workload": f"{args.graphs} graphs, n log-uniform [200, 50000], half ER avg deg 6, half BA m0=3, "
+                               "w uniform [1, 1000], K in {3..6}",
+                   "graphs": args.graphs, "vertices": total_n, "edges": total_m, "parallelism": f"replicas{world}"},
+        "build_s": round(best, 3), "labels": labels, "labels_per_s": round(labels / best, 1),
+        "autotune": {"shapes": shapes, "seconds": round(tune_s, 2), "trials": tuned["trials"]},
+        "default_shapes_build_s": round(default_s, 3), "host_graph_gen_s": round(gen_s, 1),
+        "parity": "16 graphs bit-exact vs their single builds",
+    }
+
+
+def zipf_ranks(rng, n, a, size):
+    """Vertex ranks with P(r) ~ (r + 1)^-a, by inverse-CDF sampling."""
+    c = np.cumsum(np.arange(1, n + 1, dtype=np.float64) ** -a)
+    c /= c[-1]
+    out = np.empty(size, np.int32)
+    for i in range(0, size, 1 << 24):
+        m = min(size, i + (1 << 24)) - i
+        out[i:i + m] = np.minimum(np.searchsorted(c, rng.random(m)), n - 1)
+    return out
+
+
+def run_stress(args, dist, rank, world, local):
+    """The large-graph stress workload: Chung-Lu n = 4,000,000, average degree
+    16, exponent 2.3, weights [1, 100], K = 4; grouping + generation + clean
+    within one GPU, then 100M queries with s, t Zipf(1.1) over vertex rank and
+    k uniform [1, 4], answered by the persistent serving loop (saturation) and
+    by the batched path; the two must agree."""
+    import torch
+
+    torch.cuda.set_device(local)
+    import gpu4hophl_code_gb300 as H
+
+    n, K, nq = 4_000_000, 4, args.queries if args.queries != 10_000_000 else 100_000_000
+    g = H.HostGraph.chung_lu(n, 16.0, 2.3, 10000.0, 1, 100, seed=SEED ^ 7)
+    dev = H.Graph(g)
+    t0 = time.perf_counter()
+    _, n_groups, _ = H.group_lp(dev, 1024, 100)
+    lp_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    idx = H.Index.build(dev, K)
+    build_s = time.perf_counter() - t0
+    info = idx.info()
+    rng = np.random.default_rng(17 + rank)
+    s = zipf_ranks(rng, n, 1.1, nq)
+    t = zipf_ranks(rng, n, 1.1, nq)
+    k = rng.integers(1, K + 1, nq).astype(np.int32)
+    idx.query(s[:100000], t[:100000], k[:100000])
+    barrier(dist)
+    t0 = time.perf_counter()
+    plain = idx.query(s, t, k)
+    plain_s = time.perf_counter() - t0
+    srv = H.Server()
+    gid = srv.add_index(idx)
+    r = srv.loadgen(np.full(nq, gid, np.int32), s, t, k, offered_qps=0)
+    assert r["completed"] == nq and np.array_equal(r["answers"], plain), "serving answers differ"
+    srv.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": "stress: queries/s of 100M Zipf(1.1) queries on a 4M-vertex graph K=4, serving loop",
+        "value": round(r["achieved_qps"], 1), "unit": "queries/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded Chung-Lu graph, Zipf queries)",
+        "config": {"workload": "chung_lu n=4000000 avg_deg=16 gamma=2.3 max_deg=10000 w=[1,100] K=4; "
+                               f"{nq} queries, s,t Zipf(1.1) over rank, k in [1,4]",
+                   "n": n, "edges": g.num_edges, "parallelism": f"replicas{world}"},
+        "serving": {"qps": round(r["achieved_qps"], 1), "p50_us": r["p50_us"], "p99_us": r["p99_us"]},
+        "plain_path_qps": round(nq / plain_s, 1),
+        "build": {"seconds": round(build_s, 2), "lp_s": round(lp_s, 2), "lp_groups": n_groups,
+                  "generate_s": round(info["time_generate_s"], 2), "clean_s": round(info["time_clean_s"], 2),
+                  "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
+                  "index_bytes": info["device_bytes"], "peak_bytes": info["build_peak_bytes"],
+                  "wave_splits": info["build_wave_splits"], "pool_packings": info["build_pool_compactions"]},
+        "parity": "serving answers == batched-path answers on all queries",
+    }
+
+
 def main():
     args = parse()
     dist, rank, world, local = init_dist(args)
+    if args.workload == "stress" and args.impl == "ours":
+        res = run_stress(args, dist, rank, world, local)
+        if rank == 0 and res:
+            print(json.dumps(res), flush=True)
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    if args.workload == "batched" and args.impl == "ours":
+        res = run_batched(args, dist, rank, world, local)
+        if rank == 0 and res:
+            print(json.dumps(res), flush=True)
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.impl == "reference":
         res = run_reference(args, dist, rank, world, local)
     else:

@@ -46,7 +46,9 @@ class hsdl_index_info(C.Structure):
                 ("labels", C.c_int64), ("labels_before_clean", C.c_int64), ("labels_after_clean", C.c_int64),
                 ("device_bytes", C.c_int64), ("time_generate_s", C.c_double), ("time_sort_s", C.c_double),
                 ("time_clean_s", C.c_double), ("max_row", C.c_int64), ("work_relaxations", C.c_int64),
-                ("work_join_reads", C.c_int64), ("work_labels_written", C.c_int64), ("work_clean_reads", C.c_int64)]
+                ("work_join_reads", C.c_int64), ("work_labels_written", C.c_int64), ("work_clean_reads", C.c_int64),
+                ("build_peak_bytes", C.c_int64), ("build_pool_entries", C.c_int64),
+                ("build_max_candidates", C.c_int64), ("build_wave_splits", C.c_int32), ("build_pool_compactions", C.c_int32)]
 
 
 class hsdl_serve_opts(C.Structure):
@@ -76,7 +78,7 @@ class hsdl_serve_counters(C.Structure):
 
 class hsdl_query_tuning(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("block_threads", C.c_int32), ("prefetch_ahead", C.c_int32),
-                ("lanes_per_query", C.c_int32)]
+                ("lanes_per_query", C.c_int32), ("stage_hubs", C.c_int32), ("reserved", C.c_int32)]
 
 
 P = C.c_void_p
@@ -104,6 +106,10 @@ SIGNATURES = {
     "hsdl_wave_bounds": (C.c_int, [I32, C.POINTER(hsdl_build_opts), P, I32, C.POINTER(I32)]),
     "hsdl_build": (C.c_int, [P, I32, C.POINTER(hsdl_build_opts), PP]),
     "hsdl_build_batched": (C.c_int, [I32, P, P, P, P, P, C.POINTER(hsdl_build_opts), P]),
+    "hsdl_build_autotune": (C.c_int, [P, I32, I32, C.POINTER(hsdl_build_opts), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int32)]),
+    "hsdl_build_batched_autotune": (C.c_int, [I32, P, P, P, P, P, I32, C.POINTER(hsdl_build_opts),
+                                              C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "hsdl_clean": (C.c_int, [P]),
     "hsdl_query_batch": (C.c_int, [P, I64, P, P, P, P]),
     "hsdl_query_batch_device": (C.c_int, [P, I64, P, P, P, P, P]),

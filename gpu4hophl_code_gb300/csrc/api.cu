@@ -383,6 +383,12 @@ static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
   }
   HSDL_CHECK_ARG(o->first_wave >= 0 && o->max_wave >= 0, "wave widths must be >= 0");
   HSDL_CHECK_ARG(o->device_budget_bytes >= 0, "device_budget_bytes must be >= 0");
+  HSDL_CHECK_ARG(o->block_threads == 0 || o->block_threads == 128 || o->block_threads == 256 ||
+                     o->block_threads == 512,
+                 "block_threads must be 0, 128, 256 or 512");
+  HSDL_CHECK_ARG(o->frontier_tile >= 0, "frontier_tile must be >= 0");
+  HSDL_CHECK_ARG(o->prune_lanes == 0 || o->prune_lanes == 8 || o->prune_lanes == 16 || o->prune_lanes == 32,
+                 "prune_lanes must be 0, 8, 16 or 32");
   return HSDL_OK;
 }
 
@@ -552,6 +558,11 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->work_join_reads = idx->work_join_reads;
   info->work_labels_written = idx->work_labels_written;
   info->work_clean_reads = idx->work_clean_reads;
+  info->build_peak_bytes = idx->build_peak;
+  info->build_pool_entries = idx->build_pool;
+  info->build_max_candidates = idx->build_max_cand;
+  info->build_wave_splits = idx->wave_splits;
+  info->build_pool_compactions = idx->pool_compactions;
   return HSDL_OK;
 }
 
@@ -651,9 +662,12 @@ int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* t) {
   HSDL_CHECK_ARG(t->prefetch_ahead >= 0 && t->prefetch_ahead <= 8, "prefetch_ahead must be in [0, 8]");
   HSDL_CHECK_ARG(t->lanes_per_query == 8 || t->lanes_per_query == 16 || t->lanes_per_query == 32,
                  "lanes_per_query must be 8, 16 or 32");
+  HSDL_CHECK_ARG(t->stage_hubs >= 0 && (int64_t)t->stage_hubs * t->block_threads / 32 * 4 <= 200 * 1024,
+                 "stage_hubs x warps per block x 4 B must fit in 200 KB of shared memory");
   idx->q_threads = t->block_threads;
   idx->q_ahead = t->prefetch_ahead;
   idx->q_lanes = t->lanes_per_query;
+  idx->q_stage = t->stage_hubs;
   return HSDL_OK;
 }
 
@@ -663,6 +677,8 @@ int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* t) {
   t->block_threads = idx->q_threads;
   t->prefetch_ahead = idx->q_ahead;
   t->lanes_per_query = idx->q_lanes;
+  t->stage_hubs = idx->q_stage;
+  t->reserved = 0;
   return HSDL_OK;
 }
 

@@ -128,13 +128,14 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
   int32_t Kmax = 1;
   for (int b = 0; b < B; b++) Kmax = std::max(Kmax, G[order[b]].K);
   // waves over rank layers: 1, 1, 2, 4, ... layers, at most 64 layers and
-  // 262,144 hubs per wave
+  // opts.max_wave hubs per wave (262,144 when 0)
   plan.bounds.push_back(0);
   {
+    const int64_t hub_cap = opts.max_wave > 0 ? opts.max_wave : 262144;
     int32_t r = 0, width = 1;
     while (r < max_n) {
       int32_t r1 = std::min(max_n, r + width);
-      while (r1 > r + 1 && layer_start[r1] - layer_start[r] > 262144) r1--;
+      while (r1 > r + 1 && layer_start[r1] - layer_start[r] > hub_cap) r1--;
       plan.bounds.push_back((int32_t)layer_start[r1]);
       r = r1;
       width = std::min(64, width * 2);

@@ -34,29 +34,40 @@ namespace hsdl {
 namespace {
 
 constexpr int kCleanThreads = 256;
+// Membership filter of v's hubs: one bit per hash value of a hub id, 65,536
+// bits in shared memory.  Most hubs of L[u] are not hubs of v; a clear bit
+// answers those with one shared-memory load instead of a probe sequence
+// (whose longest chain in a warp sets the warp's time).
+constexpr int kFilterBits = 16;
+constexpr int kFilterWords = (1 << kFilterBits) / 32;
 
-__device__ inline const int32_t* tab_find(const int32_t* T, uint32_t mask, int stride, int32_t w) {
+// v's hub table: keys Tk[cap] (one word per slot, so the 32 lanes of a probe
+// spread over the shared-memory banks) and rows Td[cap][K+1] of
+// hop-prefix-min distances.  Returns the slot of hub w, or -1.
+__device__ inline int tab_find(const int32_t* Tk, uint32_t mask, int32_t w) {
   uint32_t ix = table_hash((uint32_t)w, mask);
   for (uint32_t probe = 0; probe <= mask; probe++) {
-    int32_t kk = T[(int64_t)ix * stride];
-    if (kk == w) return T + (int64_t)ix * stride;
-    if (kk == kEmptyKey) return nullptr;
+    const int32_t kk = Tk[ix];
+    if (kk == w) return (int)ix;
+    if (kk == kEmptyKey) return -1;
     ix = (ix + 1) & mask;
   }
-  return nullptr;
+  return -1;
 }
 
 __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, const int64_t* __restrict__ off,
                                                          const uint32_t* __restrict__ hub,
                                                          const uint32_t* __restrict__ hd,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
-                                                         int stride, int smem_slots, int32_t* __restrict__ gscratch,
+                                                         int smem_slots, int32_t* __restrict__ gscratch,
                                                          int64_t gscratch_slots, int* __restrict__ next_v,
                                                          unsigned long long* __restrict__ reads) {
   extern __shared__ int32_t smem_tab[];
+  __shared__ uint32_t s_filter[kFilterWords];
   __shared__ int s_v;
   __shared__ int s_kept[kCleanThreads / 32];
   const int lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int R = K + 1;  // distances per slot
   unsigned long long scanned = 0;
   for (;;) {
     if (threadIdx.x == 0) s_v = atomicAdd(next_v, 1);
@@ -70,33 +81,37 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
     const int len = (int)(off[v + 1] - lo);
     int64_t cap = 8;
     while (cap < (int64_t)len + len / 2) cap <<= 1;  // load factor <= 2/3
-    int32_t* T = (cap <= smem_slots) ? smem_tab : gscratch + (int64_t)blockIdx.x * gscratch_slots * stride;
+    int32_t* Tk = (cap <= smem_slots) ? smem_tab : gscratch + (int64_t)blockIdx.x * gscratch_slots * (1 + R);
+    int32_t* Td = Tk + cap;
     const uint32_t mask = (uint32_t)cap - 1;
-    for (int64_t i = threadIdx.x; i < cap * stride; i += blockDim.x) T[i] = kInf32;
+    for (int64_t i = threadIdx.x; i < cap * (1 + R); i += blockDim.x) Tk[i] = kInf32;
+    for (int i = threadIdx.x; i < kFilterWords; i += blockDim.x) s_filter[i] = 0u;
     __syncthreads();
     for (int j = threadIdx.x; j < len; j += blockDim.x) {
       int32_t w = (int32_t)hub[lo + j];
       uint32_t x = hd[lo + j];
+      const uint32_t fb = filter_bit<kFilterBits>((uint32_t)w);
+      atomicOr(&s_filter[fb >> 5], 1u << (fb & 31));
       uint32_t ix = table_hash((uint32_t)w, mask);
       bool placed = false;
-      for (uint32_t probe = 0; probe <= mask; probe++) {  // the table is at most half full
-        int32_t old = atomicCAS(&T[(int64_t)ix * stride], kEmptyKey, w);
+      for (uint32_t probe = 0; probe <= mask; probe++) {  // the table is at most 2/3 full
+        int32_t old = atomicCAS(&Tk[ix], kEmptyKey, w);
         if (old == kEmptyKey || old == w) {
           placed = true;
           break;
         }
         ix = (ix + 1) & mask;
       }
-      if (placed) atomicMin(&T[(int64_t)ix * stride + 1 + hd_hop(x)], (int32_t)hd_dist(x));
+      if (placed) atomicMin(&Td[(int64_t)ix * R + hd_hop(x)], (int32_t)hd_dist(x));
     }
     __syncthreads();
     for (int64_t e = threadIdx.x; e < cap; e += blockDim.x) {
-      int32_t* row = T + e * stride;
-      if (row[0] == kEmptyKey) continue;
-      int32_t m = row[1];
+      if (Tk[e] == kEmptyKey) continue;
+      int32_t* row = Td + e * R;
+      int32_t m = row[0];
       for (int j = 1; j <= K; j++) {
-        m = min(m, row[1 + j]);
-        row[1 + j] = m;
+        m = min(m, row[j]);
+        row[j] = m;
       }
     }
     __syncthreads();
@@ -112,8 +127,8 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
       } else {
         long long q = LLONG_MAX;
         // hub u itself: labels of v with hub u and fewer hops
-        const int32_t* ru = tab_find(T, mask, stride, u);
-        if (ru && ru[1 + h - 1] != kInf32) q = ru[1 + h - 1];
+        const int su = tab_find(Tk, mask, u);
+        if (su >= 0 && Td[(int64_t)su * R + h - 1] != kInf32) q = Td[(int64_t)su * R + h - 1];
         if (!(q <= d)) {
           const int64_t ulo = off[u];
           const int ulen = (int)(off[u + 1] - ulo);
@@ -122,16 +137,15 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
             if (j < ulen) {
               const int w = (int)hub[ulo + j];
               const uint32_t x1 = hd[ulo + j];  // issued with the hub id: no dependent load
-              if (w != u) {
-                const int32_t* rw = tab_find(T, mask, stride, w);
-                if (rw) {
-                  int h1 = (int)hd_hop(x1);
-                  if (h1 <= h) {
-                    int32_t t = rw[1 + h - h1];
-                    if (t != kInf32) {
-                      long long c = (long long)hd_dist(x1) + t;
-                      q = c < q ? c : q;
-                    }
+              const uint32_t fb = filter_bit<kFilterBits>((uint32_t)w);
+              const int h1 = (int)hd_hop(x1);
+              if (w != u && h1 <= h && ((s_filter[fb >> 5] >> (fb & 31)) & 1u)) {
+                const int sw = tab_find(Tk, mask, w);
+                if (sw >= 0) {
+                  const int32_t t = Td[(int64_t)sw * R + h - h1];
+                  if (t != kInf32) {
+                    long long c = (long long)hd_dist(x1) + t;
+                    q = c < q ? c : q;
                   }
                 }
               }
@@ -191,18 +205,20 @@ int clean_index(hsdl_index_impl* idx) {
   cudaStream_t st = idx->stream;
   const int32_t n = idx->n, K = idx->K;
   const int sms = device_sm_count();
-  const int stride = (K + 2 <= 8) ? 8 : 16;
+  const int words = K + 2;  // per slot: key + K+1 distances
   double t0 = now_s();
-  // shared-memory table: 64 KB per block (three blocks per SM)
-  const int smem_slots = (64 * 1024) / (stride * 4);
-  const size_t smem = (size_t)smem_slots * stride * 4;
+  // shared-memory table within 64 KB per block, plus the 8 KB filter (three
+  // blocks per SM); a power-of-two slot count
+  int smem_slots = 8;
+  while ((int64_t)smem_slots * 2 * words * 4 <= 64 * 1024) smem_slots *= 2;
+  const size_t smem = (size_t)smem_slots * words * 4;
   HSDL_CUDA(cudaFuncSetAttribute(k_clean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t need_slots = 8;
   while (need_slots < idx->max_row + idx->max_row / 2) need_slots <<= 1;
   const int grid = sms * resident_blocks(k_clean, kCleanThreads, smem);
   int64_t gslots = need_slots > smem_slots ? need_slots : 0;
   DevBuf<int32_t> gscratch;
-  if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * stride, st));
+  if (gslots > 0) HSDL_TRY(gscratch.alloc((int64_t)grid * gslots * words, st));
   DevBuf<uint8_t> keep;
   DevBuf<int64_t> kept, noff;
   DevBuf<int> next;
@@ -214,7 +230,7 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_TRY(noff.alloc((int64_t)n + 1, st));
   HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
-  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p, stride,
+  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p,
                                              smem_slots, gscratch.p, gslots, next.p, reads.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));

@@ -17,7 +17,7 @@
 //              A candidate that does not beat the best distance of any earlier
 //              hop never improves the key - that is the reference's own-label
 //              dominance (generation.h:127-146).
-//      prune:  one warp per candidate joins the committed labels of v with the
+//      prune:  a group of lanes per candidate joins the committed labels of v with the
 //              hub's hop-prefix-min table (a hash table per slot, built from
 //              the hub's own labels) and keeps the candidate iff its distance
 //              is below the 2-hop query (generation.h:146-161).  Kept
@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <vector>
@@ -46,18 +47,70 @@ namespace hsdl {
 namespace {
 
 constexpr int kThreads = 256;
+// Pool regions come in size classes: class c holds 8 << c entries.  A row that
+// outgrows its region moves to the smallest class that fits; the region it
+// leaves goes on its class's free list and serves a later move.
+constexpr int kClasses = 28;
+// Per-slot membership filter of the hub's own label hubs (4,096 bits): most
+// labels of a candidate vertex name hubs the wave's hub has no label for, and
+// a clear bit settles those with one load instead of a table probe sequence.
+constexpr int kSlotFilterBits = 12;
+constexpr int kSlotFilterWords = (1 << kSlotFilterBits) / 32;
+constexpr int64_t kPoolEntryBytes = sizeof(uint64_t) + sizeof(int32_t);  // label key + parent
+// per candidate-list entry: C, both frontier buffers, and the found-label lists
+constexpr int64_t kListEntryBytes = sizeof(int2) + 2 * sizeof(int4) + 2 * sizeof(int32_t) + sizeof(uint64_t);
+
+// An instantiated CUDA graph of one wave's hop kernels, keyed by the buffers
+// and sizes its launches name.
+struct HopGraph {
+  static constexpr int kKey = 11;
+  cudaGraphExec_t exec = nullptr;
+  uintptr_t key[kKey] = {};
+  ~HopGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  template <class F>
+  int ensure(const uintptr_t* k, cudaStream_t st, F&& launches) {
+    if (exec && std::memcmp(k, key, sizeof key) == 0) return HSDL_OK;
+    if (exec) {
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    HSDL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = launches();
+    cudaGraph_t gr = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &gr);
+    if (rc != HSDL_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    HSDL_CUDA(e);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, gr, 0);
+    cudaGraphDestroy(gr);
+    HSDL_CUDA(ei);
+    std::memcpy(key, k, sizeof key);
+    return HSDL_OK;
+  }
+};
 
 struct Counters {
   unsigned long long c_count;     // candidate-list entries this wave (all hops)
   unsigned long long wl_count;    // labels found this wave
   unsigned long long overflow;    // candidate list overflowed
   unsigned long long tab_total;   // hub-table slots this wave
-  unsigned long long reloc_need;  // pool entries the commit's row moves need
   unsigned long long touched;     // rows receiving labels this wave
   unsigned long long relax;       // relaxations this wave (work counter)
   unsigned long long reads;       // committed labels read by the pruning join (work counter)
   unsigned long long hop_c[16];   // candidate-list start of each hop
   unsigned long long hop_f[16];   // frontier size of each hop
+  unsigned long long req[kClasses];     // rows moving into a region of class c this commit
+  unsigned long long freed[kClasses];   // regions of class c the moving rows leave
+  unsigned long long taken[kClasses];   // class-c requests served so far (free list first)
+  unsigned long long pushed[kClasses];  // class-c regions put on the free list so far
+  unsigned long long take_e[16];  // expansion tiles taken (dynamic work distribution)
+  unsigned long long take_p[16];  // pruning candidates taken
+  int s_hub;                      // first hub of the wave (read by the captured hop kernels)
+  int pad32;
 };
 
 // Where slot rows live.  One graph: slot s owns cand[s*n .. s*n + n) and vertex
@@ -88,6 +141,7 @@ __global__ void k_wave_init(int32_t W, int32_t s_hub, SlotMap map, uint64_t* __r
     F[slot] = make_int4(slot, hub, 0, 0);
   }
   if (slot == 0) {
+    ctr->s_hub = s_hub;
     ctr->c_count = W;
     ctr->hop_c[0] = 0;
     ctr->hop_c[1] = W;
@@ -123,7 +177,7 @@ __global__ void k_table_size(int32_t W, int32_t s_hub, const int32_t* __restrict
 __global__ void k_table_fill(int32_t W, int32_t s_hub, const int64_t* __restrict__ row_off,
                              const int32_t* __restrict__ row_len, const uint64_t* __restrict__ keys,
                              const int64_t* __restrict__ tab_off, const int32_t* __restrict__ tab_cap,
-                             int32_t* __restrict__ tab, int stride) {
+                             int32_t* __restrict__ tab, int stride, uint32_t* __restrict__ filt) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -138,6 +192,8 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, const int64_t* __restrict
     for (int j = lane; j < len; j += 32) {
       uint64_t k = keys[lo + j];
       int32_t w = (int32_t)lkey_hub(k);
+      const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
+      atomicOr(&filt[slot * kSlotFilterWords + (fb >> 5)], 1u << (fb & 31));
       uint32_t i = table_hash((uint32_t)w, mask);
       bool placed = false;
       for (int probe = 0; probe < cap; probe++) {  // tables are at most half full
@@ -170,66 +226,77 @@ __global__ void k_table_prefix(const Counters* ctr, int32_t* __restrict__ tab, i
 // ---------------------------------------------------------------------------
 // hop round: expansion
 // ---------------------------------------------------------------------------
-// Each block takes tiles of kThreads frontier entries.  Only neighbours ranked
-// below the hub are relaxed (rank prune, generation.h:107-110); rows are
-// sorted by neighbour id, so they are the suffix after the hub's id, found by
-// binary search.  The tile's relaxations are spread evenly over the block
-// through an exclusive scan of the suffix lengths.
-__global__ void __launch_bounds__(kThreads) k_expand(SlotMap map, int32_t h, int32_t K, int32_t s_hub,
-                                                     const int64_t* __restrict__ rp, const int2* __restrict__ adj,
-                                                     const int4* __restrict__ F, uint64_t* __restrict__ cand,
-                                                     int2* __restrict__ C, int64_t capC, Counters* ctr) {
-  __shared__ int64_t s_start[kThreads];
-  __shared__ int64_t s_lo[kThreads];
-  __shared__ int4 s_e[kThreads];
+// Each block takes `tiles` tiles of TPB frontier entries at a time from a
+// per-hop counter, so a block that drew heavy vertices takes fewer tiles.
+// Only neighbours ranked below the hub are relaxed (rank prune,
+// generation.h:107-110); rows are sorted by neighbour id, so they are the
+// suffix after the hub's id, found by binary search.  The tile's relaxations
+// are spread evenly over the block through an exclusive scan of the suffix
+// lengths.
+template <int TPB>
+__global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t K, int32_t tiles,
+                                                const int64_t* __restrict__ rp, const int2* __restrict__ adj,
+                                                const int4* __restrict__ F, uint64_t* __restrict__ cand,
+                                                int2* __restrict__ C, int64_t capC, Counters* ctr) {
+  __shared__ int64_t s_start[TPB];
+  __shared__ int64_t s_lo[TPB];
+  __shared__ int4 s_e[TPB];
   __shared__ int64_t s_scan[32];
+  __shared__ int64_t s_tile;
+  const int32_t s_hub = ctr->s_hub;
   const int64_t nf = (int64_t)ctr->hop_f[h - 1];
-  for (int64_t tile = blockIdx.x; tile * kThreads < nf; tile += gridDim.x) {
-    int64_t i = tile * kThreads + threadIdx.x;
-    int64_t len = 0, lo = 0;
-    int4 e = make_int4(0, 0, 0, 0);
-    if (i < nf && h <= map.hop_bound(s_hub + F[i].x, K)) {
-      e = F[i];
-      int hub = s_hub + e.x;
-      lo = rp[e.y];
-      int64_t hi = rp[e.y + 1];
-      int64_t a = lo, b = hi;
-      while (a < b) {
-        int64_t mid = (a + b) >> 1;
-        if (adj[mid].x <= hub) a = mid + 1; else b = mid;
-      }
-      lo = a;
-      len = hi - a;
-    }
-    int64_t total;
-    int64_t pre = block_exclusive_scan(len, s_scan, &total);
-    if (threadIdx.x == 0 && total) atomicAdd(&ctr->relax, (unsigned long long)total);
-    s_start[threadIdx.x] = pre;
-    s_lo[threadIdx.x] = lo;
-    s_e[threadIdx.x] = e;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int64_t)atomicAdd(&ctr->take_e[h], (unsigned long long)tiles);
     __syncthreads();
-    for (int64_t j = threadIdx.x; j < total; j += kThreads) {
-      int a = 0, b = kThreads - 1;
-      while (a < b) {
-        int mid = (a + b + 1) >> 1;
-        if (s_start[mid] <= j) a = mid; else b = mid - 1;
+    const int64_t first = s_tile;
+    if (first * TPB >= nf) break;
+    for (int64_t tile = first; tile < first + tiles && tile * TPB < nf; tile++) {
+      int64_t i = tile * TPB + threadIdx.x;
+      int64_t len = 0, lo = 0;
+      int4 e = make_int4(0, 0, 0, 0);
+      if (i < nf && h <= map.hop_bound(s_hub + F[i].x, K)) {
+        e = F[i];
+        int hub = s_hub + e.x;
+        lo = rp[e.y];
+        int64_t hi = rp[e.y + 1];
+        int64_t a = lo, b = hi;
+        while (a < b) {
+          int64_t mid = (a + b) >> 1;
+          if (adj[mid].x <= hub) a = mid + 1; else b = mid;
+        }
+        lo = a;
+        len = hi - a;
       }
-      int4 oe = s_e[a];
-      int2 nb = adj[s_lo[a] + (j - s_start[a])];
-      uint64_t key = ckey((uint32_t)oe.z + (uint32_t)nb.y, (uint32_t)h, (uint32_t)oe.y);
-      uint64_t* p = cand + map.row(oe.x) + map.local(nb.x);
-      bool app = false;
-      if (key < __ldcg((const unsigned long long*)p)) {
-        uint64_t old = atomicMin((unsigned long long*)p, (unsigned long long)key);
-        app = key < old && ckey_hop(old) != (uint32_t)h;
+      int64_t total;
+      int64_t pre = block_exclusive_scan(len, s_scan, &total);
+      if (threadIdx.x == 0 && total) atomicAdd(&ctr->relax, (unsigned long long)total);
+      s_start[threadIdx.x] = pre;
+      s_lo[threadIdx.x] = lo;
+      s_e[threadIdx.x] = e;
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < total; j += TPB) {
+        int a = 0, b = TPB - 1;
+        while (a < b) {
+          int mid = (a + b + 1) >> 1;
+          if (s_start[mid] <= j) a = mid; else b = mid - 1;
+        }
+        int4 oe = s_e[a];
+        int2 nb = adj[s_lo[a] + (j - s_start[a])];
+        uint64_t key = ckey((uint32_t)oe.z + (uint32_t)nb.y, (uint32_t)h, (uint32_t)oe.y);
+        uint64_t* p = cand + map.row(oe.x) + map.local(nb.x);
+        bool app = false;
+        if (key < __ldcg((const unsigned long long*)p)) {
+          uint64_t old = atomicMin((unsigned long long*)p, (unsigned long long)key);
+          app = key < old && ckey_hop(old) != (uint32_t)h;
+        }
+        long long pos = warp_append(app, &ctr->c_count);
+        if (app) {
+          if (pos < capC) C[pos] = make_int2(oe.x, nb.x);
+          else ctr->overflow = 1;
+        }
       }
-      long long pos = warp_append(app, &ctr->c_count);
-      if (app) {
-        if (pos < capC) C[pos] = make_int2(oe.x, nb.x);
-        else ctr->overflow = 1;
-      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -241,9 +308,17 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 }
 
 // ---------------------------------------------------------------------------
-// hop round: pruning query (one warp per candidate)
+// hop round: pruning query (a group of G lanes per candidate)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K, int32_t s_hub,
+// A candidate (slot, v) at distance d is kept iff no committed label (w, h1, d1)
+// of v with h1 <= h meets the wave hub's table entry T[w][h - h1] (the least
+// distance from the hub to w within h - h1 hops) at d1 + T <= d: the
+// reference's pruning query (generation.h:146-161).  The G lanes of a group
+// read G labels of v at a time and stop as soon as one dominates.  Warps take
+// 8 candidates per group at a time from a per-hop counter, so candidates with
+// long label lists do not hold back a statically assigned share.
+template <int G>
+__global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
                                                     const int64_t* __restrict__ row_off,
                                                     const int32_t* __restrict__ row_len,
@@ -251,66 +326,83 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
                                                     const int64_t* __restrict__ tab_off,
                                                     const int32_t* __restrict__ tab_cap,
                                                     const int32_t* __restrict__ tab, int stride,
+                                                    const uint32_t* __restrict__ filt,
                                                     int4* __restrict__ Fout, int32_t* __restrict__ wl_v,
                                                     uint64_t* __restrict__ wl_key, int32_t* __restrict__ wl_par,
                                                     Counters* ctr) {
+  constexpr int NG = 32 / G;
   const int lane = lane_id();
+  const int gi = lane / G, gl = lane % G;
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (gi * G));
+  const int32_t s_hub = ctr->s_hub;
   const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   unsigned long long scanned = 0;
-  for (int64_t i = c0 + warp; i < c1; i += nwarps) {
-    int2 e = C[i];
-    int slot = e.x, v = e.y;
-    uint64_t ck = cand[map.row(slot) + map.local(v)];
-    long long d = (long long)ckey_dist(ck);
-    long long q = LLONG_MAX;
-    int cap = tab_cap[slot];
-    if (cap > 0) {
-      const int32_t* T = tab + tab_off[slot] * stride;
-      uint32_t mask = (uint32_t)cap - 1;
-      int64_t lo = row_off[v];
-      int len = row_len[v];
-      for (int j0 = 0; j0 < len; j0 += 32) {
-        int j = j0 + lane;
-        if (j < len) {
-          uint64_t k = keys[lo + j];
-          uint32_t h1 = lkey_hop(k);
-          if ((int)h1 <= h) {
-            int32_t w = (int32_t)lkey_hub(k);
-            uint32_t ix = table_hash((uint32_t)w, mask);
-            for (int probe = 0; probe < cap; probe++) {
-              int32_t kk = T[(int64_t)ix * stride];
-              if (kk == w) {
-                int32_t t = T[(int64_t)ix * stride + 1 + (h - (int)h1)];
-                if (t != kInf32) {
-                  long long c = (long long)lkey_dist(k) + t;
-                  q = c < q ? c : q;
+  for (;;) {
+    unsigned long long took = 0;
+    if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(8 * NG));
+    took = __shfl_sync(0xffffffffu, took, 0);
+    const int64_t i0 = c0 + (int64_t)took;
+    if (i0 >= c1) break;
+    const int64_t i1 = min(c1, i0 + 8 * NG);
+    for (int64_t i = i0 + gi; i < i1; i += NG) {
+      int2 e = C[i];
+      int slot = e.x, v = e.y;
+      uint64_t ck = cand[map.row(slot) + map.local(v)];
+      long long d = (long long)ckey_dist(ck);
+      long long q = LLONG_MAX;
+      int cap = tab_cap[slot];
+      if (cap > 0) {
+        const int32_t* T = tab + tab_off[slot] * stride;
+        const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
+        uint32_t mask = (uint32_t)cap - 1;
+        int64_t lo = row_off[v];
+        int len = row_len[v];
+        for (int j0 = 0; j0 < len; j0 += G) {
+          int j = j0 + gl;
+          if (j < len) {
+            uint64_t k = keys[lo + j];
+            uint32_t h1 = lkey_hop(k);
+            const int32_t w = (int32_t)lkey_hub(k);
+            const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
+            if ((int)h1 <= h && ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u)) {
+              uint32_t ix = table_hash((uint32_t)w, mask);
+              for (int probe = 0; probe < cap; probe++) {
+                int32_t kk = T[(int64_t)ix * stride];
+                if (kk == w) {
+                  int32_t t = T[(int64_t)ix * stride + 1 + (h - (int)h1)];
+                  if (t != kInf32) {
+                    long long c = (long long)lkey_dist(k) + t;
+                    q = c < q ? c : q;
+                  }
+                  break;
                 }
-                break;
+                if (kk == kEmptyKey) break;
+                ix = (ix + 1) & mask;
               }
-              if (kk == kEmptyKey) break;
-              ix = (ix + 1) & mask;
             }
           }
+          scanned += (unsigned long long)min(G, len - j0);
+          if (__any_sync(gmask, q <= d)) break;  // already dominated
         }
-        scanned += (unsigned long long)min(32, len - j0);
-        if (__any_sync(0xffffffffu, q <= d)) break;  // already dominated
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+          long long x = __shfl_xor_sync(gmask, q, o);
+          q = x < q ? x : q;
+        }
       }
-      q = warp_min_ll(q);
-    }
-    if (d < q && lane == 0) {
-      unsigned long long p = atomicAdd(&ctr->wl_count, 1ull);
-      wl_v[p] = v;
-      wl_key[p] = lkey((uint32_t)(s_hub + slot), (uint32_t)h, (uint32_t)d);
-      wl_par[p] = (int32_t)ckey_parent(ck);
-      if (h < map.hop_bound(s_hub + slot, K)) {
-        unsigned long long f = atomicAdd(&ctr->hop_f[h], 1ull);
-        Fout[f] = make_int4(slot, v, (int)d, 0);
+      if (d < q && gl == 0) {
+        unsigned long long p = atomicAdd(&ctr->wl_count, 1ull);
+        wl_v[p] = v;
+        wl_key[p] = lkey((uint32_t)(s_hub + slot), (uint32_t)h, (uint32_t)d);
+        wl_par[p] = (int32_t)ckey_parent(ck);
+        if (h < map.hop_bound(s_hub + slot, K)) {
+          unsigned long long f = atomicAdd(&ctr->hop_f[h], 1ull);
+          Fout[f] = make_int4(slot, v, (int)d, 0);
+        }
       }
     }
   }
-  if (lane == 0 && scanned) atomicAdd(&ctr->reads, scanned);
+  if (gl == 0 && scanned) atomicAdd(&ctr->reads, scanned);
 }
 
 // ---------------------------------------------------------------------------
@@ -329,8 +421,12 @@ __global__ void k_count(const Counters* ctr, const int32_t* __restrict__ wl_v, i
 
 __device__ inline int32_t grown_cap(int64_t need) {
   int64_t c = 8;
-  while (c < 2 * need) c <<= 1;
+  while (c < need) c <<= 1;
   return (int32_t)c;
+}
+
+__device__ inline int cap_class(int64_t cap) {  // the largest class whose size fits in cap (cap >= 8)
+  return (63 - __clzll((unsigned long long)cap)) - 3;
 }
 
 __global__ void k_reserve_need(const Counters* ctr, const int32_t* __restrict__ touched,
@@ -340,15 +436,22 @@ __global__ void k_reserve_need(const Counters* ctr, const int32_t* __restrict__ 
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     int v = touched[i];
     int64_t need = (int64_t)row_len[v] + cnt[v];
-    if (need > row_cap[v]) atomicAdd(&wctr->reloc_need, (unsigned long long)grown_cap(need));
+    if (need > row_cap[v]) {
+      atomicAdd(&wctr->req[cap_class(grown_cap(need))], 1ull);
+      if (row_cap[v] >= 8) atomicAdd(&wctr->freed[cap_class(row_cap[v])], 1ull);
+    }
   }
 }
 
 // One warp per touched row: move the row to a bigger region if it overflows.
+// A class-c request takes the top free region of class c (avail[c] of them
+// were free when the commit started) or else bump-allocates at the pool's
+// tail.  The left region is staged (class, offset / 8) for k_free_push.
 __global__ void k_relocate(const Counters* ctr, const int32_t* __restrict__ touched, int64_t* __restrict__ row_off,
                            const int32_t* __restrict__ row_len, int32_t* __restrict__ row_cap,
                            const int32_t* __restrict__ cnt, uint64_t* __restrict__ keys, int32_t* __restrict__ par,
-                           unsigned long long* pool_tail) {
+                           unsigned long long* pool_tail, uint32_t* const* __restrict__ fl,
+                           const unsigned long long* __restrict__ avail, Counters* wctr, uint2* __restrict__ stage) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -357,10 +460,19 @@ __global__ void k_relocate(const Counters* ctr, const int32_t* __restrict__ touc
     int v = touched[i];
     int len = row_len[v];
     int64_t need = (int64_t)len + cnt[v];
-    if (need <= row_cap[v]) continue;
-    int32_t ncap = grown_cap(need);
+    const int32_t old_cap = row_cap[v];
+    if (need <= old_cap) {
+      if (lane == 0) stage[i] = make_uint2(0xFFFFFFFFu, 0u);
+      continue;
+    }
+    const int32_t ncap = grown_cap(need);
+    const int c = cap_class(ncap);
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(pool_tail, (unsigned long long)ncap);
+    if (lane == 0) {
+      const unsigned long long k = atomicAdd(&wctr->taken[c], 1ull);
+      if (k < avail[c]) base = (unsigned long long)fl[c][avail[c] - 1 - k] * 8ull;
+      else base = atomicAdd(pool_tail, (unsigned long long)ncap);
+    }
     base = __shfl_sync(0xffffffffu, base, 0);
     int64_t old = row_off[v];
     for (int j = lane; j < len; j += 32) {
@@ -370,7 +482,22 @@ __global__ void k_relocate(const Counters* ctr, const int32_t* __restrict__ touc
     if (lane == 0) {
       row_off[v] = (int64_t)base;
       row_cap[v] = ncap;
+      stage[i] = old_cap >= 8 ? make_uint2((uint32_t)cap_class(old_cap), (uint32_t)(old / 8))
+                              : make_uint2(0xFFFFFFFFu, 0u);
     }
+  }
+}
+
+// Puts the regions left by this commit's moves on their free lists, after the
+// entries the moves did not take: push_base[c] = avail[c] - min(req[c], avail[c]).
+__global__ void k_free_push(const Counters* ctr, const uint2* __restrict__ stage, uint32_t* const* __restrict__ fl,
+                            const unsigned long long* __restrict__ push_base, Counters* wctr) {
+  int64_t total = (int64_t)ctr->touched;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 e = stage[i];
+    if (e.x == 0xFFFFFFFFu) continue;
+    const unsigned long long pos = push_base[e.x] + atomicAdd(&wctr->pushed[e.x], 1ull);
+    fl[e.x][pos] = e.y;
   }
 }
 
@@ -384,6 +511,39 @@ __global__ void k_scatter(const Counters* ctr, const int32_t* __restrict__ wl_v,
     int64_t at = row_off[v] + pos;
     keys[at] = wl_key[p];
     par[at] = wl_par[p];
+  }
+}
+
+// Pool compaction: every row gets a fresh region just large enough for its
+// labels plus this wave's arrivals (rounded up to 8), packed in vertex order.
+__global__ void k_tight_cap(int32_t n, const int32_t* __restrict__ row_len, const int32_t* __restrict__ cnt,
+                            int64_t* __restrict__ tcap) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    int64_t need = (int64_t)row_len[v] + cnt[v];
+    tcap[v] = need > 0 ? ((need + need / 8 + 7) & ~(int64_t)7) : 0;
+  }
+}
+
+__global__ void k_compact_pool(int32_t n, const int64_t* __restrict__ noff, const int64_t* __restrict__ tcap,
+                               int64_t* __restrict__ row_off, int32_t* __restrict__ row_cap,
+                               const int32_t* __restrict__ row_len, const uint64_t* __restrict__ keys,
+                               const int32_t* __restrict__ par, uint64_t* __restrict__ nkeys,
+                               int32_t* __restrict__ npar) {
+  const int lane = lane_id();
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = warp; v < n; v += nwarps) {
+    const int64_t from = row_off[v], to = noff[v];
+    const int len = row_len[v];
+    for (int j = lane; j < len; j += 32) {
+      nkeys[to + j] = keys[from + j];
+      npar[to + j] = par[from + j];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      row_off[v] = to;
+      row_cap[v] = (int32_t)tcap[v];
+    }
   }
 }
 
@@ -468,9 +628,9 @@ std::vector<int32_t> wave_schedule(int32_t n, int32_t first, int32_t max_wave) {
 }
 
 int32_t auto_max_wave(int32_t n, int64_t budget_bytes) {
-  // dense candidate rows: max_wave * n * 8 B within a quarter of the budget,
+  // dense candidate rows: max_wave * n * 8 B within an eighth of the budget,
   // at most 2048 hubs per wave
-  int64_t avail = budget_bytes > 0 ? budget_bytes / 4 : (int64_t)16 << 30;
+  int64_t avail = budget_bytes > 0 ? budget_bytes / 8 : (int64_t)16 << 30;
   int64_t w = avail / ((int64_t)n * 8);
   w = std::max<int64_t>(1, std::min<int64_t>(2048, w));
   return (int32_t)w;
@@ -491,7 +651,7 @@ int row_max(int32_t n, const int64_t* d_off, int64_t* out, cudaStream_t st) {
 }
 
 int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx,
-                const BatchPlan* plan) {
+                const BatchPlan* plan, int32_t hub_limit) {
   const int32_t n = g->n;
   cudaStream_t st = idx->stream;
   const int sms = device_sm_count();
@@ -507,6 +667,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   } else {
     int32_t max_wave = opts.max_wave > 0 ? opts.max_wave : auto_max_wave(n, budget);
     bounds = wave_schedule(n, opts.first_wave > 0 ? opts.first_wave : 1, max_wave);
+    if (hub_limit > 0 && hub_limit < n) {  // only the first hub_limit hubs search
+      while (bounds.size() > 1 && bounds.back() > hub_limit) bounds.pop_back();
+      if (bounds.back() < hub_limit) bounds.push_back(hub_limit);
+    }
   }
   int32_t Wmax = 0;
   int64_t cand_entries = 0;  // largest wave's candidate rows
@@ -540,13 +704,22 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<uint64_t> wl_key;
   DevBuf<int64_t> tab_off;
   DevBuf<int32_t> tab_cap, tab;
+  DevBuf<uint32_t> filt;
+  // free lists of pool regions per size class (offsets / 8)
+  DevBuf<uint32_t> fl_store[kClasses];
+  DevBuf<uint32_t*> fl_ptr;
+  DevBuf<unsigned long long> fl_meta_d;
+  DevBuf<uint2> stage;
+  std::vector<uint32_t*> fl_ptrs(kClasses, nullptr);
+  std::vector<unsigned long long> fl_avail(kClasses, 0), fl_meta(2 * kClasses, 0);
   DevBuf<Counters> ctr;
   DevBuf<unsigned long long> pool_tail;
   auto release_all = [&]() {
     cand.release(); row_off.release(); row_len.release(); row_cap.release(); cnt.release(); touched.release();
     pool_keys.release(); pool_par.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
-    pool_tail.release(); d_base.release();
+    pool_tail.release(); d_base.release(); filt.release(); fl_ptr.release(); fl_meta_d.release(); stage.release();
+    for (auto& f : fl_store) f.release();
   };
   struct Guard {
     std::function<void()> f;
@@ -564,10 +737,22 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_CUDA(cudaMemsetAsync(row_len.p, 0, (size_t)row_len.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(row_cap.p, 0, (size_t)row_cap.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)cnt.bytes(), st));
-  int64_t pool_cap = std::max<int64_t>(1 << 20, (int64_t)n * 16);
+  // Memory plan: the candidate lists of a wave take at most a quarter of the
+  // budget (a wave needing more is split); the label pool takes what is left.
+  const int64_t c_limit = std::max<int64_t>(1 << 16, budget / 4 / kListEntryBytes);
+  // First pool: 1.5x the expected label count (about 0.53 sqrt(n) (deg / 10)
+  // (K / 5) labels per vertex on power-law graphs) so that it rarely grows,
+  // within a third of the budget.
+  int64_t first_pool = std::max<int64_t>(1 << 20, (int64_t)n * 16);
+  if (!plan) {
+    const double deg = (double)g->m2 / std::max(1, n);
+    const double per_v = 0.53 * std::sqrt((double)n) * std::max(1.0, deg / 10.0) * K / 5.0;
+    first_pool = std::max<int64_t>(first_pool, (int64_t)(1.5 * per_v * n));
+  }
+  int64_t pool_cap = std::max<int64_t>(1 << 16, std::min<int64_t>(first_pool, budget / 3 / kPoolEntryBytes));
   HSDL_TRY(pool_keys.alloc(pool_cap, st));
   HSDL_TRY(pool_par.alloc(pool_cap, st));
-  int64_t capC = std::max<int64_t>(1 << 20, (int64_t)n * 4);
+  int64_t capC = std::min<int64_t>(std::max<int64_t>(1 << 20, (int64_t)n * 4), c_limit);
   auto alloc_lists = [&](int64_t c) -> int {
     HSDL_TRY(Cl.alloc(c, st));
     HSDL_TRY(Fa.alloc(c, st));
@@ -580,20 +765,131 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(alloc_lists(capC));
   HSDL_TRY(tab_off.alloc(Wmax, st));
   HSDL_TRY(tab_cap.alloc(Wmax, st));
+  HSDL_TRY(filt.alloc((int64_t)Wmax * kSlotFilterWords, st));
+  HSDL_TRY(fl_ptr.alloc(kClasses, st));
+  HSDL_CUDA(cudaMemsetAsync(fl_ptr.p, 0, sizeof(uint32_t*) * kClasses, st));
+  HSDL_TRY(fl_meta_d.alloc(2 * kClasses, st));
+  HSDL_TRY(stage.alloc(n, st));
   int64_t tab_cap_entries = 1 << 16;
   HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
   HSDL_TRY(ctr.alloc(1, st));
   HSDL_TRY(pool_tail.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(pool_tail.p, 0, sizeof(unsigned long long), st));
-  Counters hc;
-  unsigned long long h_tail = 0;
-
   // grids of exactly one resident wave per kernel (grid-stride loops inside)
   const int grid = sms * resident_blocks(k_scatter, 256);
-  const int g_expand = sms * resident_blocks(k_expand, kThreads);
-  const int g_prune = sms * resident_blocks(k_prune, kThreads);
-  for (size_t wv = 0; wv + 1 < bounds.size(); wv++) {
+  // tunables: threads per expansion block, frontier entries a block takes at
+  // a time, lanes per pruning candidate (0 = chosen per wave from the mean
+  // committed row length)
+  const int tpb = (opts.block_threads == 128 || opts.block_threads == 512) ? opts.block_threads : 256;
+  const int32_t tiles = std::max(1, opts.frontier_tile / tpb);
+  const int fixed_lanes = (opts.prune_lanes == 8 || opts.prune_lanes == 16 || opts.prune_lanes == 32)
+                              ? opts.prune_lanes : 0;
+  const int g_expand = sms * (tpb == 128   ? resident_blocks(k_expand<128>, 128)
+                              : tpb == 512 ? resident_blocks(k_expand<512>, 512)
+                                           : resident_blocks(k_expand<256>, 256));
+  const int g_prune8 = sms * resident_blocks(k_prune<8>, kThreads);
+  const int g_prune16 = sms * resident_blocks(k_prune<16>, kThreads);
+  const int g_prune32 = sms * resident_blocks(k_prune<32>, kThreads);
+  int lanes = 32;
+
+  Counters hc;
+  unsigned long long h_tail = 0;
+  int64_t committed = 0;  // labels in the pool
+
+  auto fl_bytes = [&]() -> int64_t {
+    int64_t b = 0;
+    for (auto& f : fl_store) b += f.bytes();
+    return b;
+  };
+  auto held = [&]() -> int64_t {
+    return cand.bytes() + row_off.bytes() + row_len.bytes() + row_cap.bytes() + cnt.bytes() + touched.bytes() +
+           pool_keys.bytes() + pool_par.bytes() + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
+           wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() + filt.bytes() +
+           stage.bytes() + fl_bytes() +
+           idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
+  };
+  auto note_peak = [&]() { idx->build_peak = std::max(idx->build_peak, held()); };
+  note_peak();
+  // Packs every row into a fresh pool sized to the live labels plus this
+  // wave's arrivals (cnt), dropping the regions that moved-out rows left.
+  auto compact_pool = [&]() -> int {
+    DevBuf<int64_t> tcap, noff;
+    DevBuf<uint64_t> nkeys;
+    DevBuf<int32_t> npar;
+    struct Local {
+      std::function<void()> f;
+      ~Local() { f(); }
+    } local{[&]() { tcap.release(); noff.release(); nkeys.release(); npar.release(); }};
+    HSDL_TRY(tcap.alloc((int64_t)n + 1, st));
+    HSDL_TRY(noff.alloc((int64_t)n + 1, st));
+    k_tight_cap<<<grid, 256, 0, st>>>(n, row_len.p, cnt.p, tcap.p);
+    HSDL_LAUNCHED();
+    HSDL_TRY(exclusive_scan_i64(tcap.p, noff.p, n, st));
+    int64_t tot = 0;
+    HSDL_CUDA(cudaMemcpyAsync(&tot, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    HSDL_CUDA(cudaStreamSynchronize(st));
+    const int64_t cap = std::max<int64_t>(tot, 1);
+    HSDL_TRY(nkeys.alloc(cap, st));
+    HSDL_TRY(npar.alloc(cap, st));
+    idx->build_peak = std::max(idx->build_peak, held() + nkeys.bytes() + npar.bytes());
+    k_compact_pool<<<grid, 256, 0, st>>>(n, noff.p, tcap.p, row_off.p, row_cap.p, row_len.p, pool_keys.p,
+                                         pool_par.p, nkeys.p, npar.p);
+    HSDL_LAUNCHED();
+    const unsigned long long t = (unsigned long long)tot;
+    HSDL_CUDA(cudaMemcpyAsync(pool_tail.p, &t, sizeof(t), cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaStreamSynchronize(st));
+    std::swap(pool_keys.p, nkeys.p);
+    std::swap(pool_keys.cap, nkeys.cap);
+    std::swap(pool_par.p, npar.p);
+    std::swap(pool_par.cap, npar.cap);
+    pool_cap = cap;
+    idx->pool_compactions++;
+    return HSDL_OK;  // the old pool is freed with the locals
+  };
+
+
+  // The K hops of a wave (expand, mark, prune per hop) run as one CUDA graph.
+  // The kernels read the wave's first hub and their list bounds from the
+  // counters in device memory, so one graph serves every wave until a buffer
+  // it names is reallocated (then it is captured again).
+  HopGraph hops;
+  auto launch_hops = [&]() -> int {
+    for (int32_t h = 1; h <= K; h++) {
+      int4* Fin = (h & 1) ? Fa.p : Fb.p;
+      int4* Fout = (h & 1) ? Fb.p : Fa.p;
+      if (tpb == 128)
+        k_expand<128><<<g_expand, 128, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+      else if (tpb == 512)
+        k_expand<512><<<g_expand, 512, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+      else
+        k_expand<256><<<g_expand, 256, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+      HSDL_CUDA(cudaGetLastError());
+      k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
+      HSDL_CUDA(cudaGetLastError());
+#define HSDL_PRUNE(G, GRID)                                                                                  \
+  k_prune<G><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p, tab_off.p, \
+                                        tab_cap.p, tab.p, stride, filt.p, Fout, wl_v.p, wl_key.p, wl_par.p, ctr.p)
+      if (lanes == 8) HSDL_PRUNE(8, g_prune8);
+      else if (lanes == 16) HSDL_PRUNE(16, g_prune16);
+      else HSDL_PRUNE(32, g_prune32);
+#undef HSDL_PRUNE
+      HSDL_CUDA(cudaGetLastError());
+    }
+    return HSDL_OK;
+  };
+  auto run_hops = [&]() -> int {
+    const uintptr_t key[HopGraph::kKey] = {(uintptr_t)Cl.p, (uintptr_t)Fa.p, (uintptr_t)Fb.p,
+                                           (uintptr_t)cand.p, (uintptr_t)tab.p, (uintptr_t)pool_keys.p,
+                                           (uintptr_t)wl_v.p, (uintptr_t)wl_key.p, (uintptr_t)wl_par.p,
+                                           (uintptr_t)capC, (uintptr_t)lanes};
+    HSDL_TRY(hops.ensure(key, st, launch_hops));
+    HSDL_CUDA(cudaGraphLaunch(hops.exec, st));
+    launch_counter().fetch_add(3 * K, std::memory_order_relaxed);
+    return HSDL_OK;
+  };
+  for (size_t wv = 0; wv + 1 < bounds.size();) {
     const int32_t s_hub = bounds[wv], W = bounds[wv + 1] - bounds[wv];
+    bool split = false;
     int64_t wave_entries = (int64_t)W * n;
     if (plan) {
       // each slot's row is as long as its hub's graph
@@ -620,38 +916,46 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       }
       if (tab_need > 0) {
         HSDL_CUDA(cudaMemsetAsync(tab.p, 0x7F, (size_t)tab_need * stride * sizeof(int32_t), st));
+        HSDL_CUDA(cudaMemsetAsync(filt.p, 0, (size_t)W * kSlotFilterWords * sizeof(uint32_t), st));
         k_table_fill<<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(W, s_hub, row_off.p, row_len.p, pool_keys.p,
-                                                                   tab_off.p, tab_cap.p, tab.p, stride);
+                                                                   tab_off.p, tab_cap.p, tab.p, stride, filt.p);
         HSDL_LAUNCHED();
         k_table_prefix<<<grid, 256, 0, st>>>(ctr.p, tab.p, stride, K);
         HSDL_LAUNCHED();
       }
-      for (int32_t h = 1; h <= K; h++) {
-        int4* Fin = (h & 1) ? Fa.p : Fb.p;
-        int4* Fout = (h & 1) ? Fb.p : Fa.p;
-        k_expand<<<g_expand, kThreads, 0, st>>>(map, h, K, s_hub, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
-        HSDL_LAUNCHED();
-        k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
-        HSDL_LAUNCHED();
-        k_prune<<<g_prune, kThreads, 0, st>>>(map, h, K, s_hub, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p,
-                                              tab_off.p, tab_cap.p, tab.p, stride, Fout, wl_v.p, wl_key.p,
-                                              wl_par.p, ctr.p);
-        HSDL_LAUNCHED();
+      if (fixed_lanes) {
+        lanes = fixed_lanes;
+      } else {
+        const int64_t mean_row = committed / std::max<int32_t>(n, 1);
+        lanes = mean_row < 24 ? 8 : mean_row < 96 ? 16 : 32;
       }
+      HSDL_TRY(run_hops());
       HSDL_CUDA(cudaMemcpyAsync(&hc, ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
       HSDL_CUDA(cudaStreamSynchronize(st));
+      idx->build_max_cand = std::max<int64_t>(idx->build_max_cand, (int64_t)hc.c_count);
       if (!hc.overflow) break;
       // The candidate list overflowed: entries past its end were never
       // recorded, so clear this wave's slots wholesale and rerun the wave with
-      // room for twice what was asked.
+      // room for twice what was asked, or, when that would pass the lists'
+      // share of memory, as two half waves (any split of a wave in rank
+      // order generates a superset of the canonical labels).
       HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)wave_entries * sizeof(uint64_t), st));
-      capC = std::max<int64_t>(capC * 2, (int64_t)hc.c_count * 2);
+      const int64_t want = std::max<int64_t>(capC * 2, (int64_t)hc.c_count * 2);
+      if (want > c_limit && W > 1) {
+        bounds.insert(bounds.begin() + (std::ptrdiff_t)wv + 1, s_hub + W / 2);
+        idx->wave_splits++;
+        split = true;
+        break;
+      }
+      capC = want;
       HSDL_TRY(alloc_lists(capC));
+      note_peak();
       if (attempt > 40) {
         set_error("candidate list could not be sized");
         return HSDL_ERR_NOMEM;
       }
     }
+    if (split) continue;
     idx->work_relax += (int64_t)hc.relax;
     idx->work_join_reads += (int64_t)hc.reads;
     idx->work_labels_written += (int64_t)hc.wl_count;
@@ -664,30 +968,92 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_CUDA(cudaMemcpyAsync(&hc, ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
       HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
       HSDL_CUDA(cudaStreamSynchronize(st));
-      int64_t need = (int64_t)h_tail + (int64_t)hc.reloc_need;
+      // moves served from the free lists, the rest from the pool's tail
+      int64_t bump = 0;
+      for (int c = 0; c < kClasses; c++)
+        bump += (int64_t)(hc.req[c] - std::min(hc.req[c], fl_avail[c])) * ((int64_t)8 << c);
+      int64_t need = (int64_t)h_tail + bump;
+      bool packed = false;
       if (need > pool_cap) {
+        // Grow by doubling while the old and new pools fit side by side in
+        // the memory left; else grow by an eighth; else, when moved-out rows
+        // waste a third of the pool, compact it first.
+        size_t fb = 0, tb = 0;
+        HSDL_CUDA(cudaMemGetInfo(&fb, &tb));
+        const int64_t room = std::min<int64_t>((int64_t)fb, budget - held()) - ((int64_t)1 << 30);
         int64_t nc = pool_cap;
         while (nc < need) nc *= 2;
-        HSDL_TRY(pool_keys.grow(nc, (int64_t)h_tail, st));
-        HSDL_TRY(pool_par.grow(nc, (int64_t)h_tail, st));
-        pool_cap = nc;
+        if (nc * kPoolEntryBytes > room) nc = need + need / 8;
+        const int64_t live = committed;
+        if (nc * kPoolEntryBytes > room && (int64_t)h_tail - live > (int64_t)h_tail / 3) {
+          HSDL_TRY(compact_pool());
+          packed = true;
+          HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
+          HSDL_CUDA(cudaStreamSynchronize(st));
+          need = (int64_t)h_tail;  // every touched row now has room for its arrivals
+          nc = pool_cap;
+          while (nc < need) nc += nc / 8 + 1;
+        }
+        if (nc > pool_cap) {
+          // old and new pools are held together while the rows are copied
+          idx->build_peak = std::max(idx->build_peak, held() + nc * kPoolEntryBytes);
+          HSDL_TRY(pool_keys.grow(nc, (int64_t)h_tail, st));
+          HSDL_TRY(pool_par.grow(nc, (int64_t)h_tail, st));
+          pool_cap = nc;
+          note_peak();
+        }
       }
+      // free-list bookkeeping: fl_meta = {free regions at the start of the
+      // commit, where this commit's left regions go} per class
+      bool ptrs_changed = false;
+      for (int c = 0; c < kClasses; c++) {
+        if (packed) {  // packing dropped every free region; no row moves now
+          fl_avail[c] = 0;
+          fl_meta[c] = fl_meta[kClasses + c] = 0;
+          continue;
+        }
+        const unsigned long long a = fl_avail[c], used = std::min(hc.req[c], a);
+        fl_meta[c] = a;
+        fl_meta[kClasses + c] = a - used;
+        const int64_t after = (int64_t)(a - used + hc.freed[c]);
+        if (after > fl_store[c].cap) {
+          HSDL_TRY(fl_store[c].grow(std::max<int64_t>({after, 2 * fl_store[c].cap, 1024}), (int64_t)a, st));
+          fl_ptrs[c] = fl_store[c].p;
+          ptrs_changed = true;
+        }
+        fl_avail[c] = (unsigned long long)after;
+      }
+      if (ptrs_changed)
+        HSDL_CUDA(cudaMemcpyAsync(fl_ptr.p, fl_ptrs.data(), sizeof(uint32_t*) * kClasses, cudaMemcpyHostToDevice, st));
+      HSDL_CUDA(cudaMemcpyAsync(fl_meta_d.p, fl_meta.data(), sizeof(unsigned long long) * 2 * kClasses,
+                                cudaMemcpyHostToDevice, st));
       k_relocate<<<grid, 256, 0, st>>>(ctr.p, touched.p, row_off.p, row_len.p, row_cap.p, cnt.p, pool_keys.p,
-                                       pool_par.p, pool_tail.p);
+                                       pool_par.p, pool_tail.p, fl_ptr.p, fl_meta_d.p, ctr.p, stage.p);
+      HSDL_LAUNCHED();
+      k_free_push<<<grid, 256, 0, st>>>(ctr.p, stage.p, fl_ptr.p, fl_meta_d.p + kClasses, ctr.p);
       HSDL_LAUNCHED();
       k_scatter<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_off.p, row_len.p, pool_keys.p,
                                       pool_par.p);
       HSDL_LAUNCHED();
       k_clear_cnt<<<grid, 256, 0, st>>>(ctr.p, touched.p, cnt.p);
       HSDL_LAUNCHED();
+      committed += (int64_t)hc.wl_count;
     }
     k_reset<<<grid, 256, 0, st>>>(ctr.p, Cl.p, cand.p, map, capC);
     HSDL_LAUNCHED();
     idx->waves++;
+    wv++;
   }
   HSDL_CUDA(cudaStreamSynchronize(st));
   double t1 = now_s();
-  cand.release();
+  HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  idx->build_pool = (int64_t)h_tail;
+  // only the rows and the pool are needed from here on
+  cand.release(); cnt.release(); touched.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
+  wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); filt.release();
+  fl_ptr.release(); fl_meta_d.release(); stage.release();
+  for (auto& f : fl_store) f.release();
 
   // --- finalize: exact CSR with self labels, rows sorted by key ------------
   DevBuf<int64_t> flen;
@@ -702,6 +1068,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(idx->hub.alloc(total + kRowPad, st));
   HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
   HSDL_TRY(idx->par.alloc(total + kRowPad, st));
+  note_peak();
   k_final_copy<<<grid * 2, 256, 0, st>>>(n, row_off.p, row_len.p, pool_keys.p, pool_par.p, idx->off.p,
                                          idx->hub.p, idx->hd.p, idx->par.p);
   HSDL_LAUNCHED();

@@ -59,6 +59,13 @@ __device__ inline uint32_t table_hash(uint32_t w, uint32_t mask) {
   return (h ^ (h >> 15)) & mask;
 }
 
+// Bit of hub w in a membership filter of 2^bits bits (a second, independent
+// multiplicative hash; the top bits are taken).
+template <int bits>
+__device__ inline uint32_t filter_bit(uint32_t w) {
+  return (w * 0x85EBCA6Bu) >> (32 - bits);
+}
+
 // ---------------------------------------------------------------------------
 // Warp helpers.
 // ---------------------------------------------------------------------------

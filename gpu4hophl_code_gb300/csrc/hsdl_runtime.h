@@ -110,12 +110,16 @@ struct hsdl_index_impl {
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
+  int32_t q_stage = 0;        // query kernel: hub ids per warp staged in shared memory (0 = join in global memory)
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;
   double t_gen = 0, t_sort = 0, t_clean = 0;
   // work counted on the device during the build (for the roofline)
   int64_t work_relax = 0, work_join_reads = 0, work_labels_written = 0, work_clean_reads = 0;
+  // device memory of the build
+  int64_t build_peak = 0, build_pool = 0, build_max_cand = 0;
+  int32_t wave_splits = 0, pool_compactions = 0;
   cudaStream_t stream = nullptr;
   std::vector<int64_t> h_off;  // host copy of offsets (path extraction, export)
 };
@@ -144,8 +148,10 @@ struct BatchPlan {
 };
 
 // kernels / stages implemented in the .cu files
+// hub_limit > 0: only hubs [0, hub_limit) search (a partial index, used to
+// time a configuration on the widest searches)
 int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx,
-                const BatchPlan* plan = nullptr);
+                const BatchPlan* plan = nullptr, int32_t hub_limit = 0);
 int clean_index(hsdl_index_impl* idx);
 int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,
              int32_t* iterations_run);

@@ -182,6 +182,41 @@ def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block
     return o
 
 
+_TUNABLES = ("max_wave", "block_threads", "frontier_tile", "prune_lanes")
+
+
+def autotune_build(graph: "Graph", K: int, sample_hubs: int = 0, **opts) -> dict:
+    """Fastest launch shapes for building this graph (hsdl_build_autotune):
+    a dict of max_wave, block_threads, frontier_tile, prune_lanes to pass to
+    Index.build, plus 'seconds' (the sample's time) and 'trials'."""
+    o = build_opts(**opts)
+    best = C.c_double()
+    n_trials = C.c_int32()
+    check(lib().hsdl_build_autotune(graph.handle, K, sample_hubs, C.byref(o), C.byref(best), C.byref(n_trials)))
+    r = {f: getattr(o, f) for f in _TUNABLES}
+    r.update(seconds=best.value, trials=n_trials.value)
+    return r
+
+
+def autotune_build_batched(graphs, Ks, sample_graphs: int = 0, **opts) -> dict:
+    """Same for Index.build_batched (hsdl_build_batched_autotune)."""
+    B = len(graphs)
+    n = np.array([g.n for g in graphs], np.int32)
+    K = np.array(Ks, np.int32)
+    rps = (C.c_void_p * B)(*[g.row_ptr.ctypes.data for g in graphs])
+    cols = (C.c_void_p * B)(*[g.col.ctypes.data for g in graphs])
+    ws = (C.c_void_p * B)(*[g.w.ctypes.data for g in graphs])
+    o = build_opts(**opts)
+    best = C.c_double()
+    n_trials = C.c_int32()
+    check(lib().hsdl_build_batched_autotune(B, _ptr(n), C.cast(rps, C.c_void_p), C.cast(cols, C.c_void_p),
+                                            C.cast(ws, C.c_void_p), _ptr(K), sample_graphs, C.byref(o),
+                                            C.byref(best), C.byref(n_trials)))
+    r = {f: getattr(o, f) for f in _TUNABLES}
+    r.update(seconds=best.value, trials=n_trials.value)
+    return r
+
+
 def wave_bounds(n: int, **opts) -> np.ndarray:
     o = build_opts(**opts)
     cnt = C.c_int32()
@@ -274,15 +309,17 @@ class Index:
         check(lib().hsdl_extract_path(self._h, s, t, k, _ptr(e), cap, C.byref(cnt)))
         return [tuple(x) for x in e[: cnt.value].tolist()]
 
-    def set_query_tuning(self, block_threads: int = 512, prefetch_ahead: int = 0, lanes_per_query: int = 32) -> None:
-        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, lanes_per_query)
+    def set_query_tuning(self, block_threads: int = 512, prefetch_ahead: int = 0, lanes_per_query: int = 32,
+                         stage_hubs: int = 0) -> None:
+        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, lanes_per_query,
+                                stage_hubs, 0)
         check(lib().hsdl_set_query_tuning(self._h, C.byref(t)))
 
     def query_tuning(self) -> dict:
         t = N.hsdl_query_tuning()
         check(lib().hsdl_get_query_tuning(self._h, C.byref(t)))
         return {"block_threads": t.block_threads, "prefetch_ahead": t.prefetch_ahead,
-                "lanes_per_query": t.lanes_per_query}
+                "lanes_per_query": t.lanes_per_query, "stage_hubs": t.stage_hubs}
 
     def save(self, path: str) -> None:
         check(lib().hsdl_save_labels(self._h, path.encode()))

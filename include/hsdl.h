@@ -115,9 +115,9 @@ typedef struct hsdl_build_opts {
   int32_t clean;          /* 1: run hsdl_clean after generation (default 1) */
   int32_t first_wave;     /* hubs in the first wave (default 1) */
   int32_t max_wave;       /* widest wave; waves double up to it (0 = auto) */
-  int32_t block_threads;  /* threads per block of the search kernels (0 = auto) */
-  int32_t frontier_tile;  /* frontier entries per expansion tile (0 = auto) */
-  int32_t prune_lanes;    /* lanes per candidate in the pruning join (0 = auto) */
+  int32_t block_threads;  /* threads per expansion block: 128, 256 or 512 (0 = 256) */
+  int32_t frontier_tile;  /* frontier entries an expansion block takes at a time (0 = one block's worth) */
+  int32_t prune_lanes;    /* lanes per candidate in the pruning join: 8, 16 or 32 (0 = per wave, by mean row length) */
   int32_t reserved;
   int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
 } hsdl_build_opts;
@@ -135,11 +135,30 @@ int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index
  * bit-identical to hsdl_build of that graph alone.  The graphs run as one
  * disjoint union whose waves hold the same ranks of many graphs together;
  * graphs are grouped into sub-batches whose estimated labels fit
- * opts->device_budget_bytes (0 = half of free HBM).  No counterpart in the
- * reference, which builds one graph per run. */
+ * opts->device_budget_bytes (0 = half of free HBM).  A batched wave holds at
+ * most 64 rank layers and opts->max_wave hubs (0 = 262144).  No counterpart
+ * in the reference, which builds one graph per run. */
 int hsdl_build_batched(int32_t num_graphs, const int32_t* n, const int64_t* const* row_ptr,
                        const int32_t* const* col, const int32_t* const* w, const int32_t* K,
                        const hsdl_build_opts* opts, hsdl_index** out);
+
+/* Autotuning of the launch shapes above (block_threads, frontier_tile,
+ * prune_lanes, max_wave); the labels never depend on them.  Times the
+ * generation of the graph's first sample_hubs hubs (0 = 16384), the
+ * highest-ranked and widest searches, under candidate settings by coordinate
+ * descent, and writes the fastest into *opts (its other fields are kept).
+ * best_seconds and trials (either may be NULL) receive the fastest sample
+ * time and the number of timed runs.  No counterpart in the reference, whose
+ * launch shapes are compile-time constants. */
+int hsdl_build_autotune(hsdl_graph* g, int32_t K, int32_t sample_hubs, hsdl_build_opts* opts, double* best_seconds,
+                        int32_t* trials);
+/* Same for hsdl_build_batched: times batched builds of sample_graphs graphs
+ * (0 = 256) spread evenly over the input.  max_wave is then the hub cap of a
+ * batched wave. */
+int hsdl_build_batched_autotune(int32_t num_graphs, const int32_t* n, const int64_t* const* row_ptr,
+                                const int32_t* const* col, const int32_t* const* w, const int32_t* K,
+                                int32_t sample_graphs, hsdl_build_opts* opts, double* best_seconds,
+                                int32_t* trials);
 
 /* ------------------------------------------------------------------------
  * Canonical repair.  Replaces hop_constrained_clean_L
@@ -189,6 +208,10 @@ typedef struct hsdl_query_tuning {
   int32_t block_threads;
   int32_t prefetch_ahead;
   int32_t lanes_per_query;
+  int32_t stage_hubs; /* > 0: each warp copies both rows' hub ids into this many words of shared memory
+                         and joins there (pairs of rows longer than that join in global memory);
+                         0: join in global memory.  Staging uses 32 lanes per query. */
+  int32_t reserved;
 } hsdl_query_tuning;
 int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* tuning);
 int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* tuning);
@@ -220,6 +243,12 @@ typedef struct hsdl_index_info {
   int64_t work_join_reads;       /* committed labels read by the pruning joins */
   int64_t work_labels_written;   /* labels generated (before clean) */
   int64_t work_clean_reads;      /* labels read by the clean's joins */
+  /* device memory of the build */
+  int64_t build_peak_bytes;      /* most HBM the build's buffers held at once */
+  int64_t build_pool_entries;    /* label-pool entries at the end of generation (live, slack, moved-out rows) */
+  int64_t build_max_candidates;  /* longest candidate list of one wave */
+  int32_t build_wave_splits;     /* waves split in two because their candidates outgrew the memory left */
+  int32_t build_pool_compactions; /* times the label pool was packed to drop moved-out rows */
 } hsdl_index_info;
 
 int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);

@@ -66,3 +66,20 @@ def test_batched_sub_batches_under_a_tight_budget():
         ox, lx = x.export()
         oy, ly = y.export()
         assert np.array_equal(ox, oy) and np.array_equal(lx, ly)
+
+
+def test_batched_autotune_and_small_waves():
+    """The batched tuner returns valid shapes; a batch built with them, and
+    with a small hub cap per wave, still gives every graph its own labels."""
+    graphs, Ks = _batch(24, 200, 2000, 9)
+    r = H.autotune_build_batched(graphs, Ks, sample_graphs=8)
+    assert r["block_threads"] in (128, 256, 512) and r["prune_lanes"] in (0, 8, 16, 32)
+    assert r["max_wave"] in (65536, 131072, 262144, 524288) and r["trials"] >= 10
+    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    tuned = H.Index.build_batched(graphs, Ks, **shapes)
+    small = H.Index.build_batched(graphs, Ks, max_wave=256, prune_lanes=8)
+    for g, K, a, b in zip(graphs, Ks, tuned, small):
+        want = _single(g, K)
+        for ix in (a, b):
+            off, lab = ix.export()
+            assert np.array_equal(off, want[0]) and np.array_equal(lab, want[1])

@@ -55,6 +55,51 @@ def test_uncleaned_generation_matches_wave_oracle(orc, max_wave):
     assert np.array_equal(off2, canon.off) and np.array_equal(lab2, canon.lab)
 
 
+@pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes", [(128, 0, 8), (512, 4096, 16), (256, 1024, 32),
+                                                                     (256, 0, 0)])
+def test_launch_shapes_do_not_change_labels(orc, block_threads, frontier_tile, prune_lanes):
+    """The uncleaned superset depends on the wave schedule only; threads per
+    block, frontier tile and prune lanes change the time, never a label."""
+    g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=22)
+    K = 5
+    dev, idx = gpu_build(g, K, clean=False, max_wave=64, block_threads=block_threads,
+                         frontier_tile=frontier_tile, prune_lanes=prune_lanes)
+    off, lab = idx.export()
+    ref = orc.build(g, K, threads=4, wave_bounds=H.wave_bounds(g.n, max_wave=64), clean=False)
+    assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
+
+
+def test_autotune_picks_valid_shapes():
+    g = H.HostGraph.chung_lu(20000, 8, 2.2, 800, 1, 100, seed=24)
+    dev = H.Graph(g)
+    r = H.autotune_build(dev, 5, sample_hubs=4096)
+    assert r["block_threads"] in (128, 256, 512) and r["prune_lanes"] in (0, 8, 16, 32)
+    assert r["max_wave"] in (512, 1024, 2048, 4096) and r["frontier_tile"] >= 0
+    assert r["seconds"] > 0 and r["trials"] >= 10
+    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    a = H.Index.build(dev, 5, **shapes).export()
+    b = H.Index.build(dev, 5).export()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_memory_limited_build_splits_waves_and_compacts_pool(orc):
+    """Under a device budget far below what the waves want, waves whose
+    candidate lists outgrow it run as halves and the label pool is packed;
+    the cleaned labels stay the canonical set."""
+    g = H.HostGraph.chung_lu(8000, 8, 2.2, 600, 1, 100, seed=23)
+    K = 5
+    dev, idx = gpu_build(g, K, max_wave=2048, device_budget_bytes=8 << 20)
+    info = idx.info()
+    assert info["build_wave_splits"] > 0 and info["build_pool_compactions"] > 0
+    assert info["build_peak_bytes"] > 0 and info["build_max_candidates"] > 0
+    assert info["build_pool_entries"] >= info["labels_before_clean"] - g.n
+    off, lab = idx.export()
+    canon = orc.build(g, K, threads=8)
+    assert np.array_equal(off, canon.off) and np.array_equal(lab, canon.lab)
+    _, free_idx = gpu_build(g, K, max_wave=2048)
+    assert free_idx.info()["build_wave_splits"] == 0
+
+
 def test_gpu_clean_of_oracle_superset(orc):
     """hsdl_clean on an imported superset equals the oracle's clean of it."""
     g = H.HostGraph.erdos_renyi(800, 4000, 1, 50, seed=5)
@@ -171,3 +216,25 @@ def test_reference_shaped_api(orc):
     q = np.array([[1, 2, 3], [4, 5, 4], [7, 7, 0]], np.int32)
     ans, secs = H.gpu_query(ci.L, q, 4)
     assert np.array_equal(ans, orc.query(ref, q[:, 0], q[:, 1], q[:, 2]))
+
+
+@pytest.mark.parametrize("tuning", [dict(block_threads=256, stage_hubs=2048), dict(block_threads=128, stage_hubs=64),
+                                    dict(block_threads=512, lanes_per_query=16), dict(block_threads=256,
+                                                                                      lanes_per_query=8)])
+def test_query_variants_agree(orc, tuning):
+    """Every query kernel variant (shared-memory staging, including pairs of
+    rows too long for the buffer; 8/16/32 lanes per query) gives the same
+    answers as the oracle."""
+    g = H.HostGraph.chung_lu(6000, 8, 2.2, 600, 1, 100, seed=26)
+    K = 5
+    dev, idx = gpu_build(g, K)
+    rng = np.random.default_rng(8)
+    s = rng.integers(0, g.n, 50000).astype(np.int32)
+    t = rng.integers(0, g.n, 50000).astype(np.int32)
+    k = rng.integers(-1, K + 2, 50000).astype(np.int32)
+    s[:100] = t[:100]
+    base = idx.query(s, t, k)
+    assert np.array_equal(base, orc.query(orc.build(g, K, threads=4), s, t, k, threads=4))
+    idx.set_query_tuning(**tuning)
+    assert np.array_equal(idx.query(s, t, k), base)
+    assert idx.query_tuning()["stage_hubs"] == tuning.get("stage_hubs", 0)
