@@ -539,7 +539,7 @@ def run_stress(args, dist, rank, world, local):
                   "generate_s": round(info["time_generate_s"], 2), "clean_s": round(info["time_clean_s"], 2),
                   "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
                   "index_bytes": info["device_bytes"], "peak_bytes": info["build_peak_bytes"],
-                  "wave_splits": info["build_wave_splits"], "pool_packings": info["build_pool_compactions"]},
+                  "wave_splits": info["build_wave_splits"], "pool_chunks": info["build_pool_chunks"]},
         "parity": "serving answers == batched-path answers on all queries",
     }
 

@@ -99,6 +99,7 @@ void free_index(hsdl_index* idx) {
   idx->hd.release();
   idx->par.release();
   idx->qerr.release();
+  idx->wave_lo.release();
   if (idx->stream) {
     cudaStreamSynchronize(idx->stream);
     cudaStreamDestroy(idx->stream);
@@ -562,7 +563,7 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->build_pool_entries = idx->build_pool;
   info->build_max_candidates = idx->build_max_cand;
   info->build_wave_splits = idx->wave_splits;
-  info->build_pool_compactions = idx->pool_compactions;
+  info->build_pool_chunks = idx->pool_chunks;
   return HSDL_OK;
 }
 

@@ -17,6 +17,16 @@
 // (u, 0, 0), so for hub w = u the check uses v's labels of hub u with fewer
 // than h hops.  Every label is therefore decided independently.
 //
+// Wave window.  For labels generated by the wave engine, the pruning query of
+// u's search already saw every pair through a hub w of an earlier wave: both
+// w's label of u and w's label of v were committed before u's wave, and the
+// pruning rule is this rule.  What it could not see are hubs of u's own wave
+// (ranked above u), whose labels were committed with u's.  So when the index
+// records each hub's wave (wave_lo[u] = the wave's first hub), a label (u, h, d)
+// of v is checked against the hubs w of L[u] with wave_lo[u] <= w < u - the
+// tail of the sorted row - plus u's own fewer-hop labels of v.  Without the
+// record (an imported label set) the whole of L[u] is scanned.
+//
 // Kernel: one block per vertex v (persistent blocks take vertices from a work
 // counter).  The block builds v's hop-prefix-min table T_v (hash on hub id, in
 // shared memory, or in a per-block global scratch area for very long rows),
@@ -59,6 +69,7 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
                                                          const uint32_t* __restrict__ hub,
                                                          const uint32_t* __restrict__ hd,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
+                                                         const int32_t* __restrict__ wave_lo,
                                                          int smem_slots, int32_t* __restrict__ gscratch,
                                                          int64_t gscratch_slots, int* __restrict__ next_v,
                                                          unsigned long long* __restrict__ reads) {
@@ -130,16 +141,22 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
         const int su = tab_find(Tk, mask, u);
         if (su >= 0 && Td[(int64_t)su * R + h - 1] != kInf32) q = Td[(int64_t)su * R + h - 1];
         if (!(q <= d)) {
+          // L[u] is sorted by hub and its hubs are ranked at or above u, so
+          // the hubs of u's own wave are its tail: scan 32 labels at a time
+          // from the end while the chunk's first hub is still in the window.
           const int64_t ulo = off[u];
           const int ulen = (int)(off[u + 1] - ulo);
-          for (int j0 = 0; j0 < ulen; j0 += 32) {
-            int j = j0 + lane;
-            if (j < ulen) {
+          const int ws = wave_lo ? wave_lo[u] : 0;
+          for (int j1 = ulen; j1 > 0; j1 -= 32) {
+            const int j = j1 - 32 + lane;
+            bool in_window = false;
+            if (j >= 0) {
               const int w = (int)hub[ulo + j];
               const uint32_t x1 = hd[ulo + j];  // issued with the hub id: no dependent load
               const uint32_t fb = filter_bit<kFilterBits>((uint32_t)w);
               const int h1 = (int)hd_hop(x1);
-              if (w != u && h1 <= h && ((s_filter[fb >> 5] >> (fb & 31)) & 1u)) {
+              in_window = w >= ws;
+              if (in_window && w != u && h1 <= h && ((s_filter[fb >> 5] >> (fb & 31)) & 1u)) {
                 const int sw = tab_find(Tk, mask, w);
                 if (sw >= 0) {
                   const int32_t t = Td[(int64_t)sw * R + h - h1];
@@ -150,8 +167,9 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
                 }
               }
             }
-            scanned += (unsigned long long)min(32, ulen - j0);
+            scanned += (unsigned long long)min(32, j1);
             if (__any_sync(0xffffffffu, q <= d)) break;
+            if (!__shfl_sync(0xffffffffu, in_window, 0)) break;  // lane 0 holds the chunk's first label
           }
           q = warp_min_ll(q);
         }
@@ -231,7 +249,7 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
   k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p,
-                                             smem_slots, gscratch.p, gslots, next.p, reads.p);
+                                             idx->wave_lo.p, smem_slots, gscratch.p, gslots, next.p, reads.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
   int64_t total = 0;
@@ -265,6 +283,7 @@ int clean_index(hsdl_index_impl* idx) {
   gscratch.release();
   next.release();
   reads.release();
+  idx->wave_lo.release();  // the clean is done; a repeat would need the full scan
   idx->work_clean_reads += (int64_t)h_reads;
   idx->before = idx->total;
   idx->total = total;

@@ -47,10 +47,34 @@ namespace hsdl {
 namespace {
 
 constexpr int kThreads = 256;
-// Pool regions come in size classes: class c holds 8 << c entries.  A row that
-// outgrows its region moves to the smallest class that fits; the region it
-// leaves goes on its class's free list and serves a later move.
-constexpr int kClasses = 28;
+// Committed label rows are lists of doubling segments: segment i of a row
+// holds its labels [8 (2^i - 1), 8 (2^(i+1) - 1)).  A row that fills its
+// segments gets the next one; nothing is ever moved or copied, and a row's
+// capacity is below twice its length.  Segments are carved from pool chunks
+// (separate device allocations added as the pool grows) and named by a
+// 64-bit reference chunk:16 | entry:48.
+constexpr int kSegs = 25;  // 8 (2^25 - 1) >= 2^28 labels per row
+constexpr int kMaxChunks = 1024;
+constexpr int64_t kEntryMask = ((int64_t)1 << 48) - 1;
+
+__device__ inline int seg_of(int j) { return 31 - __clz((j >> 3) + 1); }
+__device__ inline int seg_first(int i) { return 8 * ((1 << i) - 1); }
+__device__ inline int segs_for(int64_t len) { return len <= 0 ? 0 : seg_of((int)(len - 1)) + 1; }
+
+struct Rows {
+  const int64_t* seg;        // [n][kSegs] segment references
+  uint64_t* const* ck;       // chunk -> label keys (hub:32 | hop:4 | distance:28)
+  int32_t* const* cp;        // chunk -> parents
+  // where label j of row v lives: chunk and entry
+  __device__ inline int64_t ref(int v, int j) const {
+    const int i = seg_of(j);
+    return __ldg(seg + (int64_t)v * kSegs + i) + (j - seg_first(i));
+  }
+  __device__ inline uint64_t key(int v, int j) const {
+    const int64_t r = ref(v, j);
+    return __ldg(((const uint64_t* const*)ck)[r >> 48] + (r & kEntryMask));
+  }
+};
 // Per-slot membership filter of the hub's own label hubs (4,096 bits): most
 // labels of a candidate vertex name hubs the wave's hub has no label for, and
 // a clear bit settles those with one load instead of a table probe sequence.
@@ -103,10 +127,8 @@ struct Counters {
   unsigned long long reads;       // committed labels read by the pruning join (work counter)
   unsigned long long hop_c[16];   // candidate-list start of each hop
   unsigned long long hop_f[16];   // frontier size of each hop
-  unsigned long long req[kClasses];     // rows moving into a region of class c this commit
-  unsigned long long freed[kClasses];   // regions of class c the moving rows leave
-  unsigned long long taken[kClasses];   // class-c requests served so far (free list first)
-  unsigned long long pushed[kClasses];  // class-c regions put on the free list so far
+  unsigned long long seg_need;     // pool entries of the segments this commit adds
+  unsigned long long seg_over;     // a row would need more than kSegs segments
   unsigned long long take_e[16];  // expansion tiles taken (dynamic work distribution)
   unsigned long long take_p[16];  // pruning candidates taken
   int s_hub;                      // first hub of the wave (read by the captured hop kernels)
@@ -174,8 +196,7 @@ __global__ void k_table_size(int32_t W, int32_t s_hub, const int32_t* __restrict
 }
 
 // Inserts every label (w, hop, d) of the hub into its table: T[w][hop] = min d.
-__global__ void k_table_fill(int32_t W, int32_t s_hub, const int64_t* __restrict__ row_off,
-                             const int32_t* __restrict__ row_len, const uint64_t* __restrict__ keys,
+__global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t* __restrict__ row_len,
                              const int64_t* __restrict__ tab_off, const int32_t* __restrict__ tab_cap,
                              int32_t* __restrict__ tab, int stride, uint32_t* __restrict__ filt) {
   int lane = lane_id();
@@ -187,10 +208,9 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, const int64_t* __restrict
     int hub = s_hub + (int)slot;
     int32_t* T = tab + tab_off[slot] * stride;
     uint32_t mask = (uint32_t)cap - 1;
-    int64_t lo = row_off[hub];
     int len = row_len[hub];
     for (int j = lane; j < len; j += 32) {
-      uint64_t k = keys[lo + j];
+      uint64_t k = rows.key(hub, j);
       int32_t w = (int32_t)lkey_hub(k);
       const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
       atomicOr(&filt[slot * kSlotFilterWords + (fb >> 5)], 1u << (fb & 31));
@@ -320,9 +340,7 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 template <int G>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
-                                                    const int64_t* __restrict__ row_off,
-                                                    const int32_t* __restrict__ row_len,
-                                                    const uint64_t* __restrict__ keys,
+                                                    Rows rows, const int32_t* __restrict__ row_len,
                                                     const int64_t* __restrict__ tab_off,
                                                     const int32_t* __restrict__ tab_cap,
                                                     const int32_t* __restrict__ tab, int stride,
@@ -355,12 +373,21 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         const int32_t* T = tab + tab_off[slot] * stride;
         const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
         uint32_t mask = (uint32_t)cap - 1;
-        int64_t lo = row_off[v];
         int len = row_len[v];
+        // lane gl of the group holds the address of the row's segment gl, so
+        // a label's address takes a shuffle instead of two dependent loads
+        const uint64_t* my_seg = nullptr;
+        if (gl < segs_for(len)) {
+          const int64_t r = __ldg(rows.seg + (int64_t)v * kSegs + gl);
+          my_seg = ((const uint64_t* const*)rows.ck)[r >> 48] + (r & kEntryMask);
+        }
         for (int j0 = 0; j0 < len; j0 += G) {
           int j = j0 + gl;
+          const int si = seg_of(min(j, len - 1));
+          const uint64_t* sp =
+              (const uint64_t*)__shfl_sync(gmask, (unsigned long long)my_seg, si < G ? si : 0, G);
           if (j < len) {
-            uint64_t k = keys[lo + j];
+            uint64_t k = si < G ? __ldg(sp + (j - seg_first(si))) : rows.key(v, j);
             uint32_t h1 = lkey_hop(k);
             const int32_t w = (int32_t)lkey_hub(k);
             const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
@@ -419,131 +446,50 @@ __global__ void k_count(const Counters* ctr, const int32_t* __restrict__ wl_v, i
   }
 }
 
-__device__ inline int32_t grown_cap(int64_t need) {
-  int64_t c = 8;
-  while (c < need) c <<= 1;
-  return (int32_t)c;
-}
-
-__device__ inline int cap_class(int64_t cap) {  // the largest class whose size fits in cap (cap >= 8)
-  return (63 - __clzll((unsigned long long)cap)) - 3;
-}
-
-__global__ void k_reserve_need(const Counters* ctr, const int32_t* __restrict__ touched,
-                               const int32_t* __restrict__ row_len, const int32_t* __restrict__ row_cap,
-                               const int32_t* __restrict__ cnt, Counters* wctr) {
+// Pool entries of the segments each touched row needs for this commit's
+// arrivals.
+__global__ void k_seg_need(const Counters* ctr, const int32_t* __restrict__ touched,
+                           const int32_t* __restrict__ row_len, const int32_t* __restrict__ cnt, Counters* wctr) {
   int64_t total = (int64_t)ctr->touched;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    int v = touched[i];
-    int64_t need = (int64_t)row_len[v] + cnt[v];
-    if (need > row_cap[v]) {
-      atomicAdd(&wctr->req[cap_class(grown_cap(need))], 1ull);
-      if (row_cap[v] >= 8) atomicAdd(&wctr->freed[cap_class(row_cap[v])], 1ull);
-    }
-  }
-}
-
-// One warp per touched row: move the row to a bigger region if it overflows.
-// A class-c request takes the top free region of class c (avail[c] of them
-// were free when the commit started) or else bump-allocates at the pool's
-// tail.  The left region is staged (class, offset / 8) for k_free_push.
-__global__ void k_relocate(const Counters* ctr, const int32_t* __restrict__ touched, int64_t* __restrict__ row_off,
-                           const int32_t* __restrict__ row_len, int32_t* __restrict__ row_cap,
-                           const int32_t* __restrict__ cnt, uint64_t* __restrict__ keys, int32_t* __restrict__ par,
-                           unsigned long long* pool_tail, uint32_t* const* __restrict__ fl,
-                           const unsigned long long* __restrict__ avail, Counters* wctr, uint2* __restrict__ stage) {
-  int lane = lane_id();
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t total = (int64_t)ctr->touched;
-  for (int64_t i = warp; i < total; i += nwarps) {
-    int v = touched[i];
-    int len = row_len[v];
-    int64_t need = (int64_t)len + cnt[v];
-    const int32_t old_cap = row_cap[v];
-    if (need <= old_cap) {
-      if (lane == 0) stage[i] = make_uint2(0xFFFFFFFFu, 0u);
+    const int v = touched[i];
+    const int64_t len = row_len[v], need = len + cnt[v];
+    const int s0 = segs_for(len), s1 = segs_for(need);
+    if (s1 > kSegs) {
+      wctr->seg_over = 1;
       continue;
     }
-    const int32_t ncap = grown_cap(need);
-    const int c = cap_class(ncap);
-    unsigned long long base = 0;
-    if (lane == 0) {
-      const unsigned long long k = atomicAdd(&wctr->taken[c], 1ull);
-      if (k < avail[c]) base = (unsigned long long)fl[c][avail[c] - 1 - k] * 8ull;
-      else base = atomicAdd(pool_tail, (unsigned long long)ncap);
-    }
-    base = __shfl_sync(0xffffffffu, base, 0);
-    int64_t old = row_off[v];
-    for (int j = lane; j < len; j += 32) {
-      keys[base + j] = keys[old + j];
-      par[base + j] = par[old + j];
-    }
-    if (lane == 0) {
-      row_off[v] = (int64_t)base;
-      row_cap[v] = ncap;
-      stage[i] = old_cap >= 8 ? make_uint2((uint32_t)cap_class(old_cap), (uint32_t)(old / 8))
-                              : make_uint2(0xFFFFFFFFu, 0u);
-    }
+    if (s1 > s0) atomicAdd(&wctr->seg_need, (unsigned long long)(seg_first(s1) - seg_first(s0)));
   }
 }
 
-// Puts the regions left by this commit's moves on their free lists, after the
-// entries the moves did not take: push_base[c] = avail[c] - min(req[c], avail[c]).
-__global__ void k_free_push(const Counters* ctr, const uint2* __restrict__ stage, uint32_t* const* __restrict__ fl,
-                            const unsigned long long* __restrict__ push_base, Counters* wctr) {
+// Carves the new segments of every touched row from the current chunk.
+__global__ void k_seg_alloc(const Counters* ctr, const int32_t* __restrict__ touched,
+                            const int32_t* __restrict__ row_len, const int32_t* __restrict__ cnt,
+                            int64_t* __restrict__ seg, int64_t chunk, unsigned long long* chunk_tail) {
   int64_t total = (int64_t)ctr->touched;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint2 e = stage[i];
-    if (e.x == 0xFFFFFFFFu) continue;
-    const unsigned long long pos = push_base[e.x] + atomicAdd(&wctr->pushed[e.x], 1ull);
-    fl[e.x][pos] = e.y;
+    const int v = touched[i];
+    const int64_t len = row_len[v], need = len + cnt[v];
+    const int s0 = segs_for(len), s1 = min(segs_for(need), kSegs);
+    if (s1 <= s0) continue;
+    const unsigned long long base =
+        atomicAdd(chunk_tail, (unsigned long long)(seg_first(s1) - seg_first(s0)));
+    for (int j = s0; j < s1; j++)
+      seg[(int64_t)v * kSegs + j] = (chunk << 48) | (int64_t)(base + (unsigned long long)(seg_first(j) - seg_first(s0)));
   }
 }
 
 __global__ void k_scatter(const Counters* ctr, const int32_t* __restrict__ wl_v, const uint64_t* __restrict__ wl_key,
-                          const int32_t* __restrict__ wl_par, const int64_t* __restrict__ row_off,
-                          int32_t* __restrict__ row_len, uint64_t* __restrict__ keys, int32_t* __restrict__ par) {
+                          const int32_t* __restrict__ wl_par, int32_t* __restrict__ row_len, Rows rows) {
   int64_t total = (int64_t)ctr->wl_count;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
-    int v = wl_v[p];
-    int pos = atomicAdd(&row_len[v], 1);
-    int64_t at = row_off[v] + pos;
-    keys[at] = wl_key[p];
-    par[at] = wl_par[p];
-  }
-}
-
-// Pool compaction: every row gets a fresh region just large enough for its
-// labels plus this wave's arrivals (rounded up to 8), packed in vertex order.
-__global__ void k_tight_cap(int32_t n, const int32_t* __restrict__ row_len, const int32_t* __restrict__ cnt,
-                            int64_t* __restrict__ tcap) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    int64_t need = (int64_t)row_len[v] + cnt[v];
-    tcap[v] = need > 0 ? ((need + need / 8 + 7) & ~(int64_t)7) : 0;
-  }
-}
-
-__global__ void k_compact_pool(int32_t n, const int64_t* __restrict__ noff, const int64_t* __restrict__ tcap,
-                               int64_t* __restrict__ row_off, int32_t* __restrict__ row_cap,
-                               const int32_t* __restrict__ row_len, const uint64_t* __restrict__ keys,
-                               const int32_t* __restrict__ par, uint64_t* __restrict__ nkeys,
-                               int32_t* __restrict__ npar) {
-  const int lane = lane_id();
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t v = warp; v < n; v += nwarps) {
-    const int64_t from = row_off[v], to = noff[v];
-    const int len = row_len[v];
-    for (int j = lane; j < len; j += 32) {
-      nkeys[to + j] = keys[from + j];
-      npar[to + j] = par[from + j];
-    }
-    __syncwarp();
-    if (lane == 0) {
-      row_off[v] = to;
-      row_cap[v] = (int32_t)tcap[v];
-    }
+    const int v = wl_v[p];
+    const int pos = atomicAdd(&row_len[v], 1);
+    const int i = seg_of(pos);
+    const int64_t r = rows.seg[(int64_t)v * kSegs + i] + (pos - seg_first(i));
+    rows.ck[r >> 48][r & kEntryMask] = wl_key[p];
+    rows.cp[r >> 48][r & kEntryMask] = wl_par[p];
   }
 }
 
@@ -571,21 +517,21 @@ __global__ void k_final_len(int32_t n, const int32_t* __restrict__ row_len, int6
     flen[v] = (int64_t)row_len[v] + 1;
 }
 
-__global__ void k_final_copy(int32_t n, const int64_t* __restrict__ row_off, const int32_t* __restrict__ row_len,
-                             const uint64_t* __restrict__ keys, const int32_t* __restrict__ par,
+__global__ void k_final_copy(int32_t n, Rows rows, const int32_t* __restrict__ row_len,
                              const int64_t* __restrict__ foff, uint32_t* __restrict__ fhub,
                              uint32_t* __restrict__ fhd, int32_t* __restrict__ fpar) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t v = warp; v < n; v += nwarps) {
-    int64_t src = row_off[v], dst = foff[v];
+    int64_t dst = foff[v];
     int len = row_len[v];
     for (int j = lane; j < len; j += 32) {
-      uint64_t k = keys[src + j];
+      const int64_t r = rows.ref((int)v, j);
+      uint64_t k = rows.ck[r >> 48][r & kEntryMask];
       fhub[dst + j] = lkey_hub(k);
       fhd[dst + j] = lkey_hd(k);
-      fpar[dst + j] = par[src + j];
+      fpar[dst + j] = rows.cp[r >> 48][r & kEntryMask];
     }
     if (lane == 0) {
       // self label (v, v, 0, 0), pushed by the reference when hub v starts
@@ -694,10 +640,14 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 
   // --- device state --------------------------------------------------------
   DevBuf<uint64_t> cand;
-  DevBuf<int64_t> row_off;
-  DevBuf<int32_t> row_len, row_cap, cnt, touched;
-  DevBuf<uint64_t> pool_keys;
-  DevBuf<int32_t> pool_par;
+  DevBuf<int32_t> row_len, cnt, touched;
+  DevBuf<int64_t> seg;  // [n][kSegs] segment references of the committed rows
+  // the label pool: chunks of keys and parents, and their device tables
+  std::vector<DevBuf<uint64_t>> chunk_keys;
+  std::vector<DevBuf<int32_t>> chunk_par;
+  DevBuf<uint64_t*> d_ck;
+  DevBuf<int32_t*> d_cp;
+  DevBuf<unsigned long long> chunk_tail;
   DevBuf<int2> Cl;
   DevBuf<int4> Fa, Fb;
   DevBuf<int32_t> wl_v, wl_par;
@@ -705,21 +655,20 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<int64_t> tab_off;
   DevBuf<int32_t> tab_cap, tab;
   DevBuf<uint32_t> filt;
-  // free lists of pool regions per size class (offsets / 8)
-  DevBuf<uint32_t> fl_store[kClasses];
-  DevBuf<uint32_t*> fl_ptr;
-  DevBuf<unsigned long long> fl_meta_d;
-  DevBuf<uint2> stage;
-  std::vector<uint32_t*> fl_ptrs(kClasses, nullptr);
-  std::vector<unsigned long long> fl_avail(kClasses, 0), fl_meta(2 * kClasses, 0);
   DevBuf<Counters> ctr;
-  DevBuf<unsigned long long> pool_tail;
+  auto release_pool = [&]() {
+    for (auto& c : chunk_keys) c.release();
+    for (auto& c : chunk_par) c.release();
+    chunk_keys.clear();
+    chunk_par.clear();
+    d_ck.release(); d_cp.release(); chunk_tail.release(); seg.release();
+  };
   auto release_all = [&]() {
-    cand.release(); row_off.release(); row_len.release(); row_cap.release(); cnt.release(); touched.release();
-    pool_keys.release(); pool_par.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
+    cand.release(); row_len.release(); cnt.release(); touched.release();
+    Cl.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
-    pool_tail.release(); d_base.release(); filt.release(); fl_ptr.release(); fl_meta_d.release(); stage.release();
-    for (auto& f : fl_store) f.release();
+    d_base.release(); filt.release();
+    release_pool();
   };
   struct Guard {
     std::function<void()> f;
@@ -728,30 +677,53 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 
   HSDL_TRY(cand.alloc(cand_entries, st));
   HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)cand.bytes(), st));
-  HSDL_TRY(row_off.alloc(n, st));
   HSDL_TRY(row_len.alloc(n, st));
-  HSDL_TRY(row_cap.alloc(n, st));
   HSDL_TRY(cnt.alloc(n, st));
   HSDL_TRY(touched.alloc(n, st));
-  HSDL_CUDA(cudaMemsetAsync(row_off.p, 0, (size_t)row_off.bytes(), st));
+  HSDL_TRY(seg.alloc((int64_t)n * kSegs, st));
   HSDL_CUDA(cudaMemsetAsync(row_len.p, 0, (size_t)row_len.bytes(), st));
-  HSDL_CUDA(cudaMemsetAsync(row_cap.p, 0, (size_t)row_cap.bytes(), st));
   HSDL_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)cnt.bytes(), st));
+  HSDL_TRY(d_ck.alloc(kMaxChunks, st));
+  HSDL_TRY(d_cp.alloc(kMaxChunks, st));
+  HSDL_TRY(chunk_tail.alloc(1, st));
+  std::vector<uint64_t*> h_ck;
+  std::vector<int32_t*> h_cp;
   // Memory plan: the candidate lists of a wave take at most a quarter of the
   // budget (a wave needing more is split); the label pool takes what is left.
   const int64_t c_limit = std::max<int64_t>(1 << 16, budget / 4 / kListEntryBytes);
-  // First pool: 1.5x the expected label count (about 0.53 sqrt(n) (deg / 10)
-  // (K / 5) labels per vertex on power-law graphs) so that it rarely grows,
-  // within a third of the budget.
-  int64_t first_pool = std::max<int64_t>(1 << 20, (int64_t)n * 16);
+  // First pool chunk: 1.4x the expected label count (about 0.53 sqrt(n)
+  // (deg / 10) (K / 5) labels per vertex on power-law graphs; segments hold
+  // rows at 1.4x their length on average), within a third of the budget.
+  // Later chunks add a quarter of the pool (at least what the commit needs).
+  int64_t first_chunk = std::max<int64_t>(1 << 20, (int64_t)n * 16);
   if (!plan) {
     const double deg = (double)g->m2 / std::max(1, n);
     const double per_v = 0.53 * std::sqrt((double)n) * std::max(1.0, deg / 10.0) * K / 5.0;
-    first_pool = std::max<int64_t>(first_pool, (int64_t)(1.5 * per_v * n));
+    first_chunk = std::max<int64_t>(first_chunk, (int64_t)(1.4 * per_v * n));
   }
-  int64_t pool_cap = std::max<int64_t>(1 << 16, std::min<int64_t>(first_pool, budget / 3 / kPoolEntryBytes));
-  HSDL_TRY(pool_keys.alloc(pool_cap, st));
-  HSDL_TRY(pool_par.alloc(pool_cap, st));
+  first_chunk = std::max<int64_t>(1 << 16, std::min<int64_t>(first_chunk, budget / 3 / kPoolEntryBytes));
+  int64_t pool_total = 0, chunk_cap = 0, chunk_used = 0;
+  auto add_chunk = [&](int64_t entries) -> int {
+    if ((int)chunk_keys.size() >= kMaxChunks) {
+      set_error("label pool: too many chunks");
+      return HSDL_ERR_NOMEM;
+    }
+    chunk_keys.emplace_back();
+    chunk_par.emplace_back();
+    HSDL_TRY(chunk_keys.back().alloc(entries, st));
+    HSDL_TRY(chunk_par.back().alloc(entries, st));
+    h_ck.push_back(chunk_keys.back().p);
+    h_cp.push_back(chunk_par.back().p);
+    HSDL_CUDA(cudaMemcpyAsync(d_ck.p, h_ck.data(), sizeof(uint64_t*) * h_ck.size(), cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemcpyAsync(d_cp.p, h_cp.data(), sizeof(int32_t*) * h_cp.size(), cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemsetAsync(chunk_tail.p, 0, sizeof(unsigned long long), st));
+    pool_total += entries;
+    chunk_cap = entries;
+    chunk_used = 0;
+    return HSDL_OK;
+  };
+  HSDL_TRY(add_chunk(first_chunk));
+  const Rows rows{seg.p, d_ck.p, d_cp.p};
   int64_t capC = std::min<int64_t>(std::max<int64_t>(1 << 20, (int64_t)n * 4), c_limit);
   auto alloc_lists = [&](int64_t c) -> int {
     HSDL_TRY(Cl.alloc(c, st));
@@ -766,15 +738,9 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(tab_off.alloc(Wmax, st));
   HSDL_TRY(tab_cap.alloc(Wmax, st));
   HSDL_TRY(filt.alloc((int64_t)Wmax * kSlotFilterWords, st));
-  HSDL_TRY(fl_ptr.alloc(kClasses, st));
-  HSDL_CUDA(cudaMemsetAsync(fl_ptr.p, 0, sizeof(uint32_t*) * kClasses, st));
-  HSDL_TRY(fl_meta_d.alloc(2 * kClasses, st));
-  HSDL_TRY(stage.alloc(n, st));
   int64_t tab_cap_entries = 1 << 16;
   HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
   HSDL_TRY(ctr.alloc(1, st));
-  HSDL_TRY(pool_tail.alloc(1, st));
-  HSDL_CUDA(cudaMemsetAsync(pool_tail.p, 0, sizeof(unsigned long long), st));
   // grids of exactly one resident wave per kernel (grid-stride loops inside)
   const int grid = sms * resident_blocks(k_scatter, 256);
   // tunables: threads per expansion block, frontier entries a block takes at
@@ -793,61 +759,16 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   int lanes = 32;
 
   Counters hc;
-  unsigned long long h_tail = 0;
   int64_t committed = 0;  // labels in the pool
 
-  auto fl_bytes = [&]() -> int64_t {
-    int64_t b = 0;
-    for (auto& f : fl_store) b += f.bytes();
-    return b;
-  };
   auto held = [&]() -> int64_t {
-    return cand.bytes() + row_off.bytes() + row_len.bytes() + row_cap.bytes() + cnt.bytes() + touched.bytes() +
-           pool_keys.bytes() + pool_par.bytes() + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
-           wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() + filt.bytes() +
-           stage.bytes() + fl_bytes() +
-           idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
+    return cand.bytes() + row_len.bytes() + cnt.bytes() + touched.bytes() + seg.bytes() +
+           pool_total * kPoolEntryBytes + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
+           wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() +
+           filt.bytes() + idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
   };
   auto note_peak = [&]() { idx->build_peak = std::max(idx->build_peak, held()); };
   note_peak();
-  // Packs every row into a fresh pool sized to the live labels plus this
-  // wave's arrivals (cnt), dropping the regions that moved-out rows left.
-  auto compact_pool = [&]() -> int {
-    DevBuf<int64_t> tcap, noff;
-    DevBuf<uint64_t> nkeys;
-    DevBuf<int32_t> npar;
-    struct Local {
-      std::function<void()> f;
-      ~Local() { f(); }
-    } local{[&]() { tcap.release(); noff.release(); nkeys.release(); npar.release(); }};
-    HSDL_TRY(tcap.alloc((int64_t)n + 1, st));
-    HSDL_TRY(noff.alloc((int64_t)n + 1, st));
-    k_tight_cap<<<grid, 256, 0, st>>>(n, row_len.p, cnt.p, tcap.p);
-    HSDL_LAUNCHED();
-    HSDL_TRY(exclusive_scan_i64(tcap.p, noff.p, n, st));
-    int64_t tot = 0;
-    HSDL_CUDA(cudaMemcpyAsync(&tot, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    HSDL_CUDA(cudaStreamSynchronize(st));
-    const int64_t cap = std::max<int64_t>(tot, 1);
-    HSDL_TRY(nkeys.alloc(cap, st));
-    HSDL_TRY(npar.alloc(cap, st));
-    idx->build_peak = std::max(idx->build_peak, held() + nkeys.bytes() + npar.bytes());
-    k_compact_pool<<<grid, 256, 0, st>>>(n, noff.p, tcap.p, row_off.p, row_cap.p, row_len.p, pool_keys.p,
-                                         pool_par.p, nkeys.p, npar.p);
-    HSDL_LAUNCHED();
-    const unsigned long long t = (unsigned long long)tot;
-    HSDL_CUDA(cudaMemcpyAsync(pool_tail.p, &t, sizeof(t), cudaMemcpyHostToDevice, st));
-    HSDL_CUDA(cudaStreamSynchronize(st));
-    std::swap(pool_keys.p, nkeys.p);
-    std::swap(pool_keys.cap, nkeys.cap);
-    std::swap(pool_par.p, npar.p);
-    std::swap(pool_par.cap, npar.cap);
-    pool_cap = cap;
-    idx->pool_compactions++;
-    return HSDL_OK;  // the old pool is freed with the locals
-  };
-
-
   // The K hops of a wave (expand, mark, prune per hop) run as one CUDA graph.
   // The kernels read the wave's first hub and their list bounds from the
   // counters in device memory, so one graph serves every wave until a buffer
@@ -867,7 +788,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());
 #define HSDL_PRUNE(G, GRID)                                                                                  \
-  k_prune<G><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, row_off.p, row_len.p, pool_keys.p, tab_off.p, \
+  k_prune<G><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,                 \
                                         tab_cap.p, tab.p, stride, filt.p, Fout, wl_v.p, wl_key.p, wl_par.p, ctr.p)
       if (lanes == 8) HSDL_PRUNE(8, g_prune8);
       else if (lanes == 16) HSDL_PRUNE(16, g_prune16);
@@ -879,7 +800,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   };
   auto run_hops = [&]() -> int {
     const uintptr_t key[HopGraph::kKey] = {(uintptr_t)Cl.p, (uintptr_t)Fa.p, (uintptr_t)Fb.p,
-                                           (uintptr_t)cand.p, (uintptr_t)tab.p, (uintptr_t)pool_keys.p,
+                                           (uintptr_t)cand.p, (uintptr_t)tab.p, (uintptr_t)seg.p,
                                            (uintptr_t)wl_v.p, (uintptr_t)wl_key.p, (uintptr_t)wl_par.p,
                                            (uintptr_t)capC, (uintptr_t)lanes};
     HSDL_TRY(hops.ensure(key, st, launch_hops));
@@ -917,8 +838,8 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       if (tab_need > 0) {
         HSDL_CUDA(cudaMemsetAsync(tab.p, 0x7F, (size_t)tab_need * stride * sizeof(int32_t), st));
         HSDL_CUDA(cudaMemsetAsync(filt.p, 0, (size_t)W * kSlotFilterWords * sizeof(uint32_t), st));
-        k_table_fill<<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(W, s_hub, row_off.p, row_len.p, pool_keys.p,
-                                                                   tab_off.p, tab_cap.p, tab.p, stride, filt.p);
+        k_table_fill<<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(W, s_hub, rows, row_len.p, tab_off.p,
+                                                                   tab_cap.p, tab.p, stride, filt.p);
         HSDL_LAUNCHED();
         k_table_prefix<<<grid, 256, 0, st>>>(ctr.p, tab.p, stride, K);
         HSDL_LAUNCHED();
@@ -963,77 +884,26 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     if (hc.wl_count > 0) {
       k_count<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, cnt.p, touched.p, ctr.p);
       HSDL_LAUNCHED();
-      k_reserve_need<<<grid, 256, 0, st>>>(ctr.p, touched.p, row_len.p, row_cap.p, cnt.p, ctr.p);
+      k_seg_need<<<grid, 256, 0, st>>>(ctr.p, touched.p, row_len.p, cnt.p, ctr.p);
       HSDL_LAUNCHED();
       HSDL_CUDA(cudaMemcpyAsync(&hc, ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-      HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
       HSDL_CUDA(cudaStreamSynchronize(st));
-      // moves served from the free lists, the rest from the pool's tail
-      int64_t bump = 0;
-      for (int c = 0; c < kClasses; c++)
-        bump += (int64_t)(hc.req[c] - std::min(hc.req[c], fl_avail[c])) * ((int64_t)8 << c);
-      int64_t need = (int64_t)h_tail + bump;
-      bool packed = false;
-      if (need > pool_cap) {
-        // Grow by doubling while the old and new pools fit side by side in
-        // the memory left; else grow by an eighth; else, when moved-out rows
-        // waste a third of the pool, compact it first.
-        size_t fb = 0, tb = 0;
-        HSDL_CUDA(cudaMemGetInfo(&fb, &tb));
-        const int64_t room = std::min<int64_t>((int64_t)fb, budget - held()) - ((int64_t)1 << 30);
-        int64_t nc = pool_cap;
-        while (nc < need) nc *= 2;
-        if (nc * kPoolEntryBytes > room) nc = need + need / 8;
-        const int64_t live = committed;
-        if (nc * kPoolEntryBytes > room && (int64_t)h_tail - live > (int64_t)h_tail / 3) {
-          HSDL_TRY(compact_pool());
-          packed = true;
-          HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
-          HSDL_CUDA(cudaStreamSynchronize(st));
-          need = (int64_t)h_tail;  // every touched row now has room for its arrivals
-          nc = pool_cap;
-          while (nc < need) nc += nc / 8 + 1;
-        }
-        if (nc > pool_cap) {
-          // old and new pools are held together while the rows are copied
-          idx->build_peak = std::max(idx->build_peak, held() + nc * kPoolEntryBytes);
-          HSDL_TRY(pool_keys.grow(nc, (int64_t)h_tail, st));
-          HSDL_TRY(pool_par.grow(nc, (int64_t)h_tail, st));
-          pool_cap = nc;
-          note_peak();
-        }
+      if (hc.seg_over) {
+        set_error("a label row outgrew 2^28 labels");
+        return HSDL_ERR_INVALID;
       }
-      // free-list bookkeeping: fl_meta = {free regions at the start of the
-      // commit, where this commit's left regions go} per class
-      bool ptrs_changed = false;
-      for (int c = 0; c < kClasses; c++) {
-        if (packed) {  // packing dropped every free region; no row moves now
-          fl_avail[c] = 0;
-          fl_meta[c] = fl_meta[kClasses + c] = 0;
-          continue;
-        }
-        const unsigned long long a = fl_avail[c], used = std::min(hc.req[c], a);
-        fl_meta[c] = a;
-        fl_meta[kClasses + c] = a - used;
-        const int64_t after = (int64_t)(a - used + hc.freed[c]);
-        if (after > fl_store[c].cap) {
-          HSDL_TRY(fl_store[c].grow(std::max<int64_t>({after, 2 * fl_store[c].cap, 1024}), (int64_t)a, st));
-          fl_ptrs[c] = fl_store[c].p;
-          ptrs_changed = true;
-        }
-        fl_avail[c] = (unsigned long long)after;
+      const int64_t need = (int64_t)hc.seg_need;
+      if (chunk_used + need > chunk_cap) {
+        // a new chunk: a quarter of the pool so far, at least this commit's need
+        HSDL_TRY(add_chunk(std::max<int64_t>(need, std::max<int64_t>(1 << 20, pool_total / 4))));
+        note_peak();
       }
-      if (ptrs_changed)
-        HSDL_CUDA(cudaMemcpyAsync(fl_ptr.p, fl_ptrs.data(), sizeof(uint32_t*) * kClasses, cudaMemcpyHostToDevice, st));
-      HSDL_CUDA(cudaMemcpyAsync(fl_meta_d.p, fl_meta.data(), sizeof(unsigned long long) * 2 * kClasses,
-                                cudaMemcpyHostToDevice, st));
-      k_relocate<<<grid, 256, 0, st>>>(ctr.p, touched.p, row_off.p, row_len.p, row_cap.p, cnt.p, pool_keys.p,
-                                       pool_par.p, pool_tail.p, fl_ptr.p, fl_meta_d.p, ctr.p, stage.p);
+      k_seg_alloc<<<grid, 256, 0, st>>>(ctr.p, touched.p, row_len.p, cnt.p, seg.p, (int64_t)chunk_keys.size() - 1,
+                                        chunk_tail.p);
       HSDL_LAUNCHED();
-      k_free_push<<<grid, 256, 0, st>>>(ctr.p, stage.p, fl_ptr.p, fl_meta_d.p + kClasses, ctr.p);
-      HSDL_LAUNCHED();
-      k_scatter<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_off.p, row_len.p, pool_keys.p,
-                                      pool_par.p);
+      chunk_used += need;
+      idx->build_pool += need;
+      k_scatter<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_len.p, rows);
       HSDL_LAUNCHED();
       k_clear_cnt<<<grid, 256, 0, st>>>(ctr.p, touched.p, cnt.p);
       HSDL_LAUNCHED();
@@ -1046,14 +916,19 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   }
   HSDL_CUDA(cudaStreamSynchronize(st));
   double t1 = now_s();
-  HSDL_CUDA(cudaMemcpyAsync(&h_tail, pool_tail.p, sizeof(h_tail), cudaMemcpyDeviceToHost, st));
-  HSDL_CUDA(cudaStreamSynchronize(st));
-  idx->build_pool = (int64_t)h_tail;
+  idx->pool_chunks = (int32_t)chunk_keys.size();
+  {
+    // each hub's wave, for the clean's wave window
+    std::vector<int32_t> h_lo((size_t)n, 0);
+    for (size_t i = 0; i + 1 < bounds.size(); i++)
+      for (int32_t u = bounds[i]; u < bounds[i + 1] && u < n; u++) h_lo[u] = bounds[i];
+    HSDL_TRY(idx->wave_lo.alloc(n, st));
+    HSDL_CUDA(cudaMemcpyAsync(idx->wave_lo.p, h_lo.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaStreamSynchronize(st));
+  }
   // only the rows and the pool are needed from here on
   cand.release(); cnt.release(); touched.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
   wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); filt.release();
-  fl_ptr.release(); fl_meta_d.release(); stage.release();
-  for (auto& f : fl_store) f.release();
 
   // --- finalize: exact CSR with self labels, rows sorted by key ------------
   DevBuf<int64_t> flen;
@@ -1069,8 +944,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
   HSDL_TRY(idx->par.alloc(total + kRowPad, st));
   note_peak();
-  k_final_copy<<<grid * 2, 256, 0, st>>>(n, row_off.p, row_len.p, pool_keys.p, pool_par.p, idx->off.p,
-                                         idx->hub.p, idx->hd.p, idx->par.p);
+  k_final_copy<<<grid * 2, 256, 0, st>>>(n, rows, row_len.p, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p);
   HSDL_LAUNCHED();
   flen.release();
   release_all();

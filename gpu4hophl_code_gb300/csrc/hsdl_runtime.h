@@ -107,6 +107,7 @@ struct hsdl_index_impl {
   DevBuf<uint32_t> hd;    // hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
+  DevBuf<int32_t> wave_lo;    // generated, not yet cleaned: first hub of each hub's wave
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
@@ -119,7 +120,7 @@ struct hsdl_index_impl {
   int64_t work_relax = 0, work_join_reads = 0, work_labels_written = 0, work_clean_reads = 0;
   // device memory of the build
   int64_t build_peak = 0, build_pool = 0, build_max_cand = 0;
-  int32_t wave_splits = 0, pool_compactions = 0;
+  int32_t wave_splits = 0, pool_chunks = 0;
   cudaStream_t stream = nullptr;
   std::vector<int64_t> h_off;  // host copy of offsets (path extraction, export)
 };

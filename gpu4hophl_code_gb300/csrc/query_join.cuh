@@ -33,38 +33,43 @@ __device__ inline long long lane_merge(const uint32_t* A, int la, const uint32_t
   long long best = INT_MAX;
   const int tot = la + lb;
   const int d0 = (int)(((int64_t)tot * gl) / G), d1 = (int)(((int64_t)tot * (gl + 1)) / G);
-  if (d0 < d1) {
-    // merge-path split of diagonal d0: ia labels of A precede it
-    int lo = max(0, d0 - lb), hi = min(d0, la);
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
+  // merge-path split of diagonal d0: ia labels of A precede it.  The search
+  // runs a fixed number of halvings (enough for the longest range) so the
+  // lanes of a group stay converged.
+  int lo = max(0, d0 - lb), hi = min(d0, la);
+  for (int span = la; span > 0; span >>= 1) {
+    if (lo < hi) {
+      const int mid = (lo + hi) >> 1;
       if (A[mid] <= B[d0 - 1 - mid]) lo = mid + 1; else hi = mid;
     }
-    int ia = lo, ib = d0 - lo;
-    uint32_t wa = ia < la ? A[ia] : 0xFFFFFFFFu;
-    uint32_t wb = ib < lb ? B[ib] : 0xFFFFFFFFu;
-    for (int step = d0; step < d1; step++) {
-      if (ia < la && (ib >= lb || wa <= wb)) {
-        if (wa == wb) {
-          const uint32_t xa = __ldg(Ahd + ia);
-          const int h1 = (int)hd_hop(xa);
-          if (h1 <= k) {
-            const long long da = hd_dist(xa);
-            for (int p = ib; p < lb && B[p] == wa; p++) {
-              const uint32_t xb = __ldg(Bhd + p);
-              if (h1 + (int)hd_hop(xb) > k) break;  // rows are hop-sorted within a hub
-              const long long c = da + hd_dist(xb);
-              best = c < best ? c : best;
-            }
-          }
+  }
+  int ia = lo, ib = d0 - lo;
+  uint32_t wa = ia < la ? A[ia] : 0xFFFFFFFFu;
+  uint32_t wb = ib < lb ? B[ib] : 0xFFFFFFFFu;
+  // Each step takes the smaller head (A's on ties) and loads its successor
+  // through one selected pointer, with no branch on which side moved.
+  for (int step = d0; step < d1; step++) {
+    const bool take_a = ia < la && (ib >= lb || wa <= wb);
+    if (take_a && wa == wb) {  // a common hub: B's run of it starts at ib
+      const uint32_t xa = __ldg(Ahd + ia);
+      const int h1 = (int)hd_hop(xa);
+      if (h1 <= k) {
+        const long long da = hd_dist(xa);
+        for (int p = ib; p < lb && B[p] == wa; p++) {
+          const uint32_t xb = __ldg(Bhd + p);
+          if (h1 + (int)hd_hop(xb) > k) break;  // rows are hop-sorted within a hub
+          const long long c = da + hd_dist(xb);
+          best = c < best ? c : best;
         }
-        ia++;
-        wa = ia < la ? A[ia] : 0xFFFFFFFFu;
-      } else {
-        ib++;
-        wb = ib < lb ? B[ib] : 0xFFFFFFFFu;
       }
     }
+    ia += take_a ? 1 : 0;
+    ib += take_a ? 0 : 1;
+    const int at = take_a ? ia : ib;
+    const int lim = take_a ? la : lb;
+    const uint32_t nxt = at < lim ? (take_a ? A : B)[at] : 0xFFFFFFFFu;
+    wa = take_a ? nxt : wa;
+    wb = take_a ? wb : nxt;
   }
   return best;
 }

@@ -245,10 +245,10 @@ typedef struct hsdl_index_info {
   int64_t work_clean_reads;      /* labels read by the clean's joins */
   /* device memory of the build */
   int64_t build_peak_bytes;      /* most HBM the build's buffers held at once */
-  int64_t build_pool_entries;    /* label-pool entries at the end of generation (live, slack, moved-out rows) */
+  int64_t build_pool_entries;    /* label-pool entries the generation's rows occupied (labels and row slack) */
   int64_t build_max_candidates;  /* longest candidate list of one wave */
   int32_t build_wave_splits;     /* waves split in two because their candidates outgrew the memory left */
-  int32_t build_pool_compactions; /* times the label pool was packed to drop moved-out rows */
+  int32_t build_pool_chunks;     /* device allocations the label pool grew by */
 } hsdl_index_info;
 
 int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);
