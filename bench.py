@@ -120,23 +120,42 @@ def make_queries(n, nq, K, seed):
 
 
 def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
-    """Per query: the hub ids of both label rows (4 B each; the join must read
-    every one), the four row offsets (32 B), the (s,t,k) record in (12 B) and
-    the answer out (4 B).  The hop/distance words read on hub matches are not
-    counted, so the achieved bandwidth derived from this is a lower bound."""
+    """Per query: the label keys of both rows (8 B each: hub:32 | hop:4 |
+    distance:28; the join must read every one), the four row offsets (32 B),
+    the (s,t,k) record in (12 B) and the answer out (4 B)."""
     ln = np.diff(off)
     rows = ln[s].astype(np.int64) + ln[t].astype(np.int64)
     rows[s == t] = 0
-    return int(4 * rows.sum() + 48 * len(s))
+    return int(8 * rows.sum() + 48 * len(s))
+
+
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_query_traffic_chung_lu_1m_10Mq.md")
+
+
+def captured_traffic(args):
+    """DRAM bytes (read + write) of one k_query launch of this workload, as
+    captured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass)
+    and recorded in the profile summary's line 'traffic per launch: <bytes>'.
+    Only the default workload (n = 1M, 10M queries) was captured; None for
+    any other."""
+    if args.n != 1_000_000 or args.queries != 10_000_000 or args.K != 5:
+        return None
+    try:
+        for line in open(TRAFFIC_PROFILE):
+            if line.lower().startswith("traffic per launch:"):
+                return int(line.split(":", 1)[1].strip().split()[0].replace(",", ""))
+    except OSError:
+        pass
+    return None
 
 
 def build_algorithmic_bytes(info: dict) -> int:
     """Bytes the build must move, from the work the device counted: per
     relaxation an 8-byte adjacency entry and an 8-byte candidate key; per
     committed label read by a pruning join an 8-byte key; per label generated
-    an 8-byte key and a 4-byte parent; per label read by the clean's joins a
-    4-byte hub id and a 4-byte hop|distance word; per final label a read and a
-    write of 12 bytes (sort and compaction)."""
+    an 8-byte key and a 4-byte parent; per label read by the clean's joins an
+    8-byte key; per final label a read and a write of 12 bytes (sort and
+    compaction)."""
     return int(16 * info["work_relaxations"] + 8 * info["work_join_reads"] + 12 * info["work_labels_written"] +
                8 * info["work_clean_reads"] + 24 * info["labels"])
 
@@ -294,7 +313,7 @@ def run_ours(args, dist, rank, world, local):
         achieved = bytes_per_launch / (kernel_ms / 1000.0 / args.steps) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
-                "traffic": None,
+                "traffic": captured_traffic(args),
                 "kernel": "k_query", "algorithmic_bytes_per_launch": bytes_per_launch,
                 "bytes_per_query": round(bytes_per_launch / args.queries, 1)}
         cpu = None

@@ -78,7 +78,7 @@ class hsdl_serve_counters(C.Structure):
 
 class hsdl_query_tuning(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("block_threads", C.c_int32), ("prefetch_ahead", C.c_int32),
-                ("lanes_per_query", C.c_int32), ("stage_hubs", C.c_int32), ("reserved", C.c_int32)]
+                ("lanes_per_query", C.c_int32)]
 
 
 P = C.c_void_p

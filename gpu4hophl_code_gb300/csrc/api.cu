@@ -95,8 +95,7 @@ void free_index(hsdl_index* idx) {
   if (!idx) return;
   if (idx->stream) cudaStreamSynchronize(idx->stream);
   idx->off.release();
-  idx->hub.release();
-  idx->hd.release();
+  idx->key.release();
   idx->par.release();
   idx->qerr.release();
   idx->wave_lo.release();
@@ -107,18 +106,14 @@ void free_index(hsdl_index* idx) {
   delete idx;
 }
 
-// Copies row v of an index to the host as packed keys (hub << 32 | hd) and
-// parents.
+// Copies row v of an index to the host as label keys and parents.
 int fetch_row(hsdl_index* idx, int32_t v, std::vector<uint64_t>& k, std::vector<int32_t>& p) {
   int64_t lo = idx->h_off[v], len = idx->h_off[v + 1] - lo;
   k.resize(len);
   p.resize(len);
   if (len == 0) return HSDL_OK;
-  std::vector<uint32_t> hb(len), hd(len);
-  HSDL_CUDA(cudaMemcpy(hb.data(), idx->hub.p + lo, len * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-  HSDL_CUDA(cudaMemcpy(hd.data(), idx->hd.p + lo, len * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  HSDL_CUDA(cudaMemcpy(k.data(), idx->key.p + lo, len * sizeof(uint64_t), cudaMemcpyDeviceToHost));
   HSDL_CUDA(cudaMemcpy(p.data(), idx->par.p + lo, len * sizeof(int32_t), cudaMemcpyDeviceToHost));
-  for (int64_t i = 0; i < len; i++) k[i] = ((uint64_t)hb[i] << 32) | hd[i];
   return HSDL_OK;
 }
 
@@ -127,7 +122,7 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
   HSDL_CHECK_ARG(offsets && offsets[0] == 0, "offsets[0] must be 0");
   int64_t total = offsets[n];
-  std::vector<uint32_t> hub((size_t)total), hd((size_t)total);
+  std::vector<uint64_t> keys((size_t)total);
   std::vector<int32_t> par((size_t)total);
   int64_t mr = 0;
   for (int32_t v = 0; v < n; v++) {
@@ -143,8 +138,7 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
       HSDL_CHECK_ARG(i == offsets[v] || prev < key,
                      "row " + std::to_string(v) + " is not sorted by (hub, hop, distance)");
       prev = key;
-      hub[i] = lkey_hub(key);
-      hd[i] = lkey_hd(key);
+      keys[i] = key;
       par[i] = x.parent_vertex;
     }
   }
@@ -155,13 +149,11 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   idx->max_row = mr;
   cudaStream_t st = idx->stream;
   HSDL_TRY(idx->off.alloc((int64_t)n + 1, st));
-  HSDL_TRY(idx->hub.alloc(total + kRowPad, st));
-  HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->key.alloc(total + kRowPad, st));
   HSDL_TRY(idx->par.alloc(total + kRowPad, st));
   HSDL_CUDA(cudaMemcpyAsync(idx->off.p, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
   if (total > 0) {
-    HSDL_CUDA(cudaMemcpyAsync(idx->hub.p, hub.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, st));
-    HSDL_CUDA(cudaMemcpyAsync(idx->hd.p, hd.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemcpyAsync(idx->key.p, keys.data(), sizeof(uint64_t) * total, cudaMemcpyHostToDevice, st));
     HSDL_CUDA(cudaMemcpyAsync(idx->par.p, par.data(), sizeof(int32_t) * total, cudaMemcpyHostToDevice, st));
   }
   HSDL_CUDA(cudaStreamSynchronize(st));
@@ -550,7 +542,7 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->labels = idx->total;
   info->labels_before_clean = idx->before;
   info->labels_after_clean = idx->after;
-  info->device_bytes = idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
+  info->device_bytes = idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
   info->time_generate_s = idx->t_gen;
   info->time_sort_s = idx->t_sort;
   info->time_clean_s = idx->t_clean;
@@ -570,19 +562,18 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
 int hsdl_export(hsdl_index* idx, int64_t* offsets, hsdl_label* labels) {
   HSDL_CHECK_ARG(idx && offsets && (idx->total == 0 || labels), "null argument");
   HSDL_CUDA(cudaStreamSynchronize(idx->stream));
-  std::vector<uint32_t> hub((size_t)idx->total), hd((size_t)idx->total);
+  std::vector<uint64_t> keys((size_t)idx->total);
   std::vector<int32_t> par((size_t)idx->total);
   if (idx->total > 0) {
-    HSDL_CUDA(cudaMemcpy(hub.data(), idx->hub.p, sizeof(uint32_t) * idx->total, cudaMemcpyDeviceToHost));
-    HSDL_CUDA(cudaMemcpy(hd.data(), idx->hd.p, sizeof(uint32_t) * idx->total, cudaMemcpyDeviceToHost));
+    HSDL_CUDA(cudaMemcpy(keys.data(), idx->key.p, sizeof(uint64_t) * idx->total, cudaMemcpyDeviceToHost));
     HSDL_CUDA(cudaMemcpy(par.data(), idx->par.p, sizeof(int32_t) * idx->total, cudaMemcpyDeviceToHost));
   }
   std::copy(idx->h_off.begin(), idx->h_off.end(), offsets);
   for (int64_t i = 0; i < idx->total; i++) {
-    labels[i].hub_vertex = (int32_t)hub[i];
+    labels[i].hub_vertex = (int32_t)lkey_hub(keys[i]);
     labels[i].parent_vertex = par[i];
-    labels[i].hop = (int32_t)hd_hop(hd[i]);
-    labels[i].distance = (int32_t)hd_dist(hd[i]);
+    labels[i].hop = (int32_t)lkey_hop(keys[i]);
+    labels[i].distance = (int32_t)lkey_dist(keys[i]);
   }
   return HSDL_OK;
 }
@@ -663,12 +654,9 @@ int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* t) {
   HSDL_CHECK_ARG(t->prefetch_ahead >= 0 && t->prefetch_ahead <= 8, "prefetch_ahead must be in [0, 8]");
   HSDL_CHECK_ARG(t->lanes_per_query == 8 || t->lanes_per_query == 16 || t->lanes_per_query == 32,
                  "lanes_per_query must be 8, 16 or 32");
-  HSDL_CHECK_ARG(t->stage_hubs >= 0 && (int64_t)t->stage_hubs * t->block_threads / 32 * 4 <= 200 * 1024,
-                 "stage_hubs x warps per block x 4 B must fit in 200 KB of shared memory");
   idx->q_threads = t->block_threads;
   idx->q_ahead = t->prefetch_ahead;
   idx->q_lanes = t->lanes_per_query;
-  idx->q_stage = t->stage_hubs;
   return HSDL_OK;
 }
 
@@ -678,8 +666,6 @@ int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* t) {
   t->block_threads = idx->q_threads;
   t->prefetch_ahead = idx->q_ahead;
   t->lanes_per_query = idx->q_lanes;
-  t->stage_hubs = idx->q_stage;
-  t->reserved = 0;
   return HSDL_OK;
 }
 

@@ -34,23 +34,21 @@ int upload_graph(int32_t n, const int64_t* rp, const int32_t* col, const int32_t
 
 namespace {
 
-__global__ void k_split(int64_t nu, const int64_t* __restrict__ uoff, const uint32_t* __restrict__ uhub,
-                        const uint32_t* __restrict__ uhd, const int32_t* __restrict__ upar,
-                        const int32_t* __restrict__ comp, const int32_t* __restrict__ lid,
-                        const int64_t* __restrict__ dst, uint32_t* const* __restrict__ dhub,
-                        uint32_t* const* __restrict__ dhd, int32_t* const* __restrict__ dpar) {
+__global__ void k_split(int64_t nu, const int64_t* __restrict__ uoff, const uint64_t* __restrict__ ukey,
+                        const int32_t* __restrict__ upar, const int32_t* __restrict__ comp,
+                        const int32_t* __restrict__ lid, const int64_t* __restrict__ dst,
+                        uint64_t* const* __restrict__ dkey, int32_t* const* __restrict__ dpar) {
   const int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t u = warp; u < nu; u += nwarps) {
     const int g = comp[u];
     const int64_t lo = uoff[u], len = uoff[u + 1] - lo, at = dst[u];
-    uint32_t* oh = dhub[g];
-    uint32_t* ox = dhd[g];
+    uint64_t* ok = dkey[g];
     int32_t* op = dpar[g];
     for (int64_t j = lane; j < len; j += 32) {
-      oh[at + j] = (uint32_t)lid[uhub[lo + j]];
-      ox[at + j] = uhd[lo + j];
+      const uint64_t k = ukey[lo + j];
+      ok[at + j] = ((uint64_t)(uint32_t)lid[lkey_hub(k)] << 32) | lkey_hd(k);  // hub id inside its own graph
       op[at + j] = lid[upar[lo + j]];
     }
   }
@@ -200,7 +198,7 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
     }
   }
   std::vector<hsdl_index*> outs(B, nullptr);
-  std::vector<uint32_t*> ph(B), px(B);
+  std::vector<uint64_t*> pk(B);
   std::vector<int32_t*> pp(B);
   for (int pos = 0; pos < B && rc == HSDL_OK; pos++) {
     rc = new_index_handle(&outs[pos]);
@@ -208,27 +206,24 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
     hsdl_index* x = outs[pos];
     const int32_t gn = G[order[pos]].n;
     const int64_t tot = goff[pos][gn];
-    if ((rc = x->off.alloc((int64_t)gn + 1, st)) != HSDL_OK || (rc = x->hub.alloc(tot + kRowPad, st)) != HSDL_OK ||
-        (rc = x->hd.alloc(tot + kRowPad, st)) != HSDL_OK || (rc = x->par.alloc(tot + kRowPad, st)) != HSDL_OK)
+    if ((rc = x->off.alloc((int64_t)gn + 1, st)) != HSDL_OK || (rc = x->key.alloc(tot + kRowPad, st)) != HSDL_OK ||
+        (rc = x->par.alloc(tot + kRowPad, st)) != HSDL_OK)
       break;
     cudaMemcpyAsync(x->off.p, goff[pos].data(), sizeof(int64_t) * (gn + 1), cudaMemcpyHostToDevice, st);
-    ph[pos] = x->hub.p;
-    px[pos] = x->hd.p;
+    pk[pos] = x->key.p;
     pp[pos] = x->par.p;
   }
   DevBuf<int64_t> d_dst;
-  DevBuf<uint32_t*> d_ph, d_px;
+  DevBuf<uint64_t*> d_pk;
   DevBuf<int32_t*> d_pp;
-  if (rc == HSDL_OK && (rc = d_dst.alloc(nu, st)) == HSDL_OK && (rc = d_ph.alloc(B, st)) == HSDL_OK &&
-      (rc = d_px.alloc(B, st)) == HSDL_OK && (rc = d_pp.alloc(B, st)) == HSDL_OK) {
+  if (rc == HSDL_OK && (rc = d_dst.alloc(nu, st)) == HSDL_OK && (rc = d_pk.alloc(B, st)) == HSDL_OK &&
+      (rc = d_pp.alloc(B, st)) == HSDL_OK) {
     cudaMemcpyAsync(d_dst.p, dst.data(), sizeof(int64_t) * nu, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d_ph.p, ph.data(), sizeof(uint32_t*) * B, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d_px.p, px.data(), sizeof(uint32_t*) * B, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_pk.p, pk.data(), sizeof(uint64_t*) * B, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_pp.p, pp.data(), sizeof(int32_t*) * B, cudaMemcpyHostToDevice, st);
     const int sms = device_sm_count();
-    k_split<<<sms * resident_blocks(k_split, 256), 256, 0, st>>>(nu, uidx->off.p, uidx->hub.p, uidx->hd.p,
-                                                                 uidx->par.p, d_comp.p, d_lid.p, d_dst.p, d_ph.p,
-                                                                 d_px.p, d_pp.p);
+    k_split<<<sms * resident_blocks(k_split, 256), 256, 0, st>>>(nu, uidx->off.p, uidx->key.p, uidx->par.p,
+                                                                 d_comp.p, d_lid.p, d_dst.p, d_pk.p, d_pp.p);
     launch_counter().fetch_add(1);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -238,8 +233,7 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
     }
   }
   d_dst.release();
-  d_ph.release();
-  d_px.release();
+  d_pk.release();
   d_pp.release();
   if (rc == HSDL_OK) {
     for (int pos = 0; pos < B; pos++) {
@@ -247,7 +241,7 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
       const GraphIn& gi = G[order[pos]];
       // the buffers were allocated on the union's stream; they now belong to
       // the graph's own stream (the union stream has been synchronised)
-      x->off.st = x->hub.st = x->hd.st = x->par.st = x->stream;
+      x->off.st = x->key.st = x->par.st = x->stream;
       x->n = gi.n;
       x->K = gi.K;
       x->cleaned = true;

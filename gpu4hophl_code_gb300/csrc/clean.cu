@@ -66,8 +66,7 @@ __device__ inline int tab_find(const int32_t* Tk, uint32_t mask, int32_t w) {
 }
 
 __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, const int64_t* __restrict__ off,
-                                                         const uint32_t* __restrict__ hub,
-                                                         const uint32_t* __restrict__ hd,
+                                                         const uint64_t* __restrict__ key,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
                                                          const int32_t* __restrict__ wave_lo,
                                                          int smem_slots, int32_t* __restrict__ gscratch,
@@ -99,8 +98,9 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
     for (int i = threadIdx.x; i < kFilterWords; i += blockDim.x) s_filter[i] = 0u;
     __syncthreads();
     for (int j = threadIdx.x; j < len; j += blockDim.x) {
-      int32_t w = (int32_t)hub[lo + j];
-      uint32_t x = hd[lo + j];
+      const uint64_t kv = key[lo + j];
+      int32_t w = (int32_t)lkey_hub(kv);
+      uint32_t x = lkey_hd(kv);
       const uint32_t fb = filter_bit<kFilterBits>((uint32_t)w);
       atomicOr(&s_filter[fb >> 5], 1u << (fb & 31));
       uint32_t ix = table_hash((uint32_t)w, mask);
@@ -128,8 +128,9 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
     __syncthreads();
     int my_kept = 0;
     for (int i = wid; i < len; i += nw) {
-      int u = (int)hub[lo + i];
-      uint32_t x = hd[lo + i];
+      const uint64_t kv = key[lo + i];
+      int u = (int)lkey_hub(kv);
+      uint32_t x = lkey_hd(kv);
       int h = (int)hd_hop(x);
       long long d = (long long)hd_dist(x);
       bool keepit;
@@ -151,8 +152,9 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
             const int j = j1 - 32 + lane;
             bool in_window = false;
             if (j >= 0) {
-              const int w = (int)hub[ulo + j];
-              const uint32_t x1 = hd[ulo + j];  // issued with the hub id: no dependent load
+              const uint64_t k1 = key[ulo + j];
+              const int w = (int)lkey_hub(k1);
+              const uint32_t x1 = lkey_hd(k1);
               const uint32_t fb = filter_bit<kFilterBits>((uint32_t)w);
               const int h1 = (int)hd_hop(x1);
               in_window = w >= ws;
@@ -189,10 +191,10 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
   }
 }
 
-__global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint32_t* __restrict__ hub,
-                          const uint32_t* __restrict__ hd, const int32_t* __restrict__ par,
+__global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint64_t* __restrict__ key,
+                          const int32_t* __restrict__ par,
                           const uint8_t* __restrict__ keep, const int64_t* __restrict__ noff,
-                          uint32_t* __restrict__ nhub, uint32_t* __restrict__ nhd, int32_t* __restrict__ npar) {
+                          uint64_t* __restrict__ nkey, int32_t* __restrict__ npar) {
   const int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -204,8 +206,7 @@ __global__ void k_compact(int32_t n, const int64_t* __restrict__ off, const uint
       unsigned b = __ballot_sync(0xffffffffu, k);
       if (k) {
         int64_t at = dst + __popc(b & ((1u << lane) - 1));
-        nhub[at] = hub[lo + j];
-        nhd[at] = hd[lo + j];
+        nkey[at] = key[lo + j];
         npar[at] = par[lo + j];
       }
       dst += __popc(b);
@@ -248,7 +249,7 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_TRY(noff.alloc((int64_t)n + 1, st));
   HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
-  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->hub.p, idx->hd.p, keep.p, kept.p,
+  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->key.p, keep.p, kept.p,
                                              idx->wave_lo.p, smem_slots, gscratch.p, gslots, next.p, reads.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
@@ -257,26 +258,21 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_CUDA(cudaMemcpyAsync(&total, noff.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaMemcpyAsync(&h_reads, reads.p, sizeof(h_reads), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
-  DevBuf<uint32_t> nhub, nhd;
+  DevBuf<uint64_t> nkey;
   DevBuf<int32_t> npar;
-  HSDL_TRY(nhub.alloc(total + kRowPad, st));
-  HSDL_TRY(nhd.alloc(total + kRowPad, st));
+  HSDL_TRY(nkey.alloc(total + kRowPad, st));
   HSDL_TRY(npar.alloc(total + kRowPad, st));
-  k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p, keep.p, noff.p, nhub.p,
-                                     nhd.p, npar.p);
+  k_compact<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->key.p, idx->par.p, keep.p, noff.p, nkey.p, npar.p);
   HSDL_LAUNCHED();
   HSDL_CUDA(cudaStreamSynchronize(st));
   std::swap(idx->off.p, noff.p);
   std::swap(idx->off.cap, noff.cap);
-  std::swap(idx->hub.p, nhub.p);
-  std::swap(idx->hub.cap, nhub.cap);
-  std::swap(idx->hd.p, nhd.p);
-  std::swap(idx->hd.cap, nhd.cap);
+  std::swap(idx->key.p, nkey.p);
+  std::swap(idx->key.cap, nkey.cap);
   std::swap(idx->par.p, npar.p);
   std::swap(idx->par.cap, npar.cap);
   noff.release();
-  nhub.release();
-  nhd.release();
+  nkey.release();
   npar.release();
   keep.release();
   kept.release();

@@ -381,35 +381,62 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
           const int64_t r = __ldg(rows.seg + (int64_t)v * kSegs + gl);
           my_seg = ((const uint64_t* const*)rows.ck)[r >> 48] + (r & kEntryMask);
         }
-        for (int j0 = 0; j0 < len; j0 += G) {
-          int j = j0 + gl;
-          const int si = seg_of(min(j, len - 1));
+        // Each lane takes two adjacent labels (one 16-byte load; pairs never
+        // straddle a segment, whose sizes and starts are even) and loads the
+        // next pair before it probes the current one.
+        auto load_pair = [&](int jp, uint64_t& k0, uint64_t& k1) {
+          const int si = seg_of(min(jp, len - 1));
           const uint64_t* sp =
               (const uint64_t*)__shfl_sync(gmask, (unsigned long long)my_seg, si < G ? si : 0, G);
-          if (j < len) {
-            uint64_t k = si < G ? __ldg(sp + (j - seg_first(si))) : rows.key(v, j);
-            uint32_t h1 = lkey_hop(k);
-            const int32_t w = (int32_t)lkey_hub(k);
-            const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
-            if ((int)h1 <= h && ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u)) {
-              uint32_t ix = table_hash((uint32_t)w, mask);
-              for (int probe = 0; probe < cap; probe++) {
-                int32_t kk = T[(int64_t)ix * stride];
-                if (kk == w) {
-                  int32_t t = T[(int64_t)ix * stride + 1 + (h - (int)h1)];
-                  if (t != kInf32) {
-                    long long c = (long long)lkey_dist(k) + t;
-                    q = c < q ? c : q;
-                  }
-                  break;
-                }
-                if (kk == kEmptyKey) break;
-                ix = (ix + 1) & mask;
-              }
+          k0 = k1 = ~0ull;  // hop field 15: never within the bound
+          if (jp < len) {
+            if (si < G) {
+              const uint4 x = __ldg((const uint4*)(sp + (jp - seg_first(si))));
+              k0 = ((uint64_t)x.y << 32) | x.x;
+              k1 = ((uint64_t)x.w << 32) | x.z;
+            } else {
+              k0 = rows.key(v, jp);
+              if (jp + 1 < len) k1 = rows.key(v, jp + 1);
             }
+            if (jp + 1 >= len) k1 = ~0ull;
           }
-          scanned += (unsigned long long)min(G, len - j0);
+        };
+        auto probe = [&](uint64_t k, uint32_t fw) {
+          const int32_t w = (int32_t)lkey_hub(k);
+          const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
+          if (!((fw >> (fb & 31)) & 1u)) return;
+          const int h1 = (int)lkey_hop(k);
+          uint32_t ix = table_hash((uint32_t)w, mask);
+          for (int pr = 0; pr < cap; pr++) {
+            const int32_t kk = T[(int64_t)ix * stride];
+            if (kk == w) {
+              const int32_t t = T[(int64_t)ix * stride + 1 + (h - h1)];
+              if (t != kInf32) {
+                const long long c = (long long)lkey_dist(k) + t;
+                q = c < q ? c : q;
+              }
+              return;
+            }
+            if (kk == kEmptyKey) return;
+            ix = (ix + 1) & mask;
+          }
+        };
+        uint64_t a0, a1;
+        load_pair(2 * gl, a0, a1);
+        for (int j0 = 0; j0 < len; j0 += 2 * G) {
+          uint64_t b0, b1;
+          load_pair(j0 + 2 * G + 2 * gl, b0, b1);
+          const bool c0 = (int)lkey_hop(a0) <= h, c1 = (int)lkey_hop(a1) <= h;
+          const uint32_t fb0 = filter_bit<kSlotFilterBits>(lkey_hub(a0));
+          const uint32_t fb1 = filter_bit<kSlotFilterBits>(lkey_hub(a1));
+          const uint32_t f0 = c0 ? __ldg(Fl + (fb0 >> 5)) : 0u;
+          const uint32_t f1 = c1 ? __ldg(Fl + (fb1 >> 5)) : 0u;
+          if (c0) probe(a0, f0);
+          if (c1) probe(a1, f1);
+          scanned += (unsigned long long)min(2 * G, len - j0);
           if (__any_sync(gmask, q <= d)) break;  // already dominated
+          a0 = b0;
+          a1 = b1;
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) {
@@ -518,8 +545,8 @@ __global__ void k_final_len(int32_t n, const int32_t* __restrict__ row_len, int6
 }
 
 __global__ void k_final_copy(int32_t n, Rows rows, const int32_t* __restrict__ row_len,
-                             const int64_t* __restrict__ foff, uint32_t* __restrict__ fhub,
-                             uint32_t* __restrict__ fhd, int32_t* __restrict__ fpar) {
+                             const int64_t* __restrict__ foff, uint64_t* __restrict__ fkey,
+                             int32_t* __restrict__ fpar) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -528,16 +555,13 @@ __global__ void k_final_copy(int32_t n, Rows rows, const int32_t* __restrict__ r
     int len = row_len[v];
     for (int j = lane; j < len; j += 32) {
       const int64_t r = rows.ref((int)v, j);
-      uint64_t k = rows.ck[r >> 48][r & kEntryMask];
-      fhub[dst + j] = lkey_hub(k);
-      fhd[dst + j] = lkey_hd(k);
+      fkey[dst + j] = rows.ck[r >> 48][r & kEntryMask];
       fpar[dst + j] = rows.cp[r >> 48][r & kEntryMask];
     }
     if (lane == 0) {
       // self label (v, v, 0, 0), pushed by the reference when hub v starts
       // (generation.h:74-85)
-      fhub[dst + len] = (uint32_t)v;
-      fhd[dst + len] = hd_pack(0, 0);
+      fkey[dst + len] = lkey((uint32_t)v, 0, 0);
       fpar[dst + len] = (int32_t)v;
     }
   }
@@ -765,7 +789,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     return cand.bytes() + row_len.bytes() + cnt.bytes() + touched.bytes() + seg.bytes() +
            pool_total * kPoolEntryBytes + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
            wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() +
-           filt.bytes() + idx->off.bytes() + idx->hub.bytes() + idx->hd.bytes() + idx->par.bytes();
+           filt.bytes() + idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
   };
   auto note_peak = [&]() { idx->build_peak = std::max(idx->build_peak, held()); };
   note_peak();
@@ -940,17 +964,16 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   int64_t total = 0;
   HSDL_CUDA(cudaMemcpyAsync(&total, idx->off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
-  HSDL_TRY(idx->hub.alloc(total + kRowPad, st));
-  HSDL_TRY(idx->hd.alloc(total + kRowPad, st));
+  HSDL_TRY(idx->key.alloc(total + kRowPad, st));
   HSDL_TRY(idx->par.alloc(total + kRowPad, st));
   note_peak();
-  k_final_copy<<<grid * 2, 256, 0, st>>>(n, rows, row_len.p, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p);
+  k_final_copy<<<grid * 2, 256, 0, st>>>(n, rows, row_len.p, idx->off.p, idx->key.p, idx->par.p);
   HSDL_LAUNCHED();
   flen.release();
   release_all();
   int64_t mr = 0;
   HSDL_TRY(row_max(n, idx->off.p, &mr, st));
-  HSDL_TRY(sort_rows(n, idx->off.p, idx->hub.p, idx->hd.p, idx->par.p, mr, st));
+  HSDL_TRY(sort_rows(n, idx->off.p, idx->key.p, idx->par.p, mr, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
   double t2 = now_s();
   idx->n = n;

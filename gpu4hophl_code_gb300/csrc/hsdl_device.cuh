@@ -13,10 +13,10 @@ namespace hsdl {
 // Unsigned order of the key is exactly the reference's label order
 // (hub asc, hop asc, distance asc; compare_hop_constrained_two_hop_label,
 // CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:373-387),
-// so sorting keys sorts labels.  A resident index stores the two halves as
-// separate arrays (hub[], hd[] = hop:4|distance:28) so that joins can stream
-// 4-byte hub ids and fetch hop and distance only on a hub match;
-// parent_vertex is kept in a parallel int32 array.  Limits: vertex ids < 2^28
+// so sorting keys sorts labels.  A resident index stores one key per label
+// (a join gets hop and distance with the hub id, no dependent load), with
+// parent_vertex in a parallel int32 array; hd = hop:4|distance:28 is the
+// key's low word.  Limits: vertex ids < 2^28
 // (the reference itself stops at 10^7, generation.h:528-532), hop <= 14,
 // distance < 2^28 (K * max edge weight < 2^28).
 //

@@ -93,25 +93,24 @@ struct hsdl_graph_impl {
   std::vector<int64_t> h_rp;  // host copy of row_ptr (for sizing decisions)
 };
 
-// A built (or imported) label index resident in HBM, per-vertex CSR in three
-// parallel arrays: hub[] (hub_vertex), hd[] (hop:4 | distance:28) and par[]
-// (parent_vertex).  Rows are sorted by (hub, hd), the reference's order.
-// The arrays carry kRowPad spare entries at the end so that 16-byte aligned
-// bulk copies of any row stay inside the allocation.
+// A built (or imported) label index resident in HBM, per-vertex CSR in two
+// parallel arrays: key[] (hub:32 | hop:4 | distance:28, one 8-byte word per
+// label, so a join gets hop and distance with the hub id) and par[]
+// (parent_vertex).  Rows are sorted by key, the reference's order.  The
+// arrays carry kRowPad spare entries at the end so that 16-byte aligned bulk
+// copies of any row stay inside the allocation.
 constexpr int64_t kRowPad = 8;
 struct hsdl_index_impl {
   int32_t n = 0, K = 0;
   bool cleaned = false;
   DevBuf<int64_t> off;    // n+1
-  DevBuf<uint32_t> hub;   // hub_vertex
-  DevBuf<uint32_t> hd;    // hop:4 | distance:28
+  DevBuf<uint64_t> key;   // hub:32 | hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
   DevBuf<int32_t> wave_lo;    // generated, not yet cleaned: first hub of each hub's wave
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
-  int32_t q_stage = 0;        // query kernel: hub ids per warp staged in shared memory (0 = join in global memory)
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;
@@ -159,8 +158,7 @@ int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st);
 int query_error(hsdl_index_impl* idx);  // HSDL_ERR_TIMEOUT (and clears) if a query kernel flagged one
-int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int32_t* par, int64_t max_row,
-              cudaStream_t st);
+int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int64_t max_row, cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total
 
 }  // namespace hsdl

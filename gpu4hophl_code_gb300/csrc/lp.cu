@@ -115,15 +115,17 @@ __global__ void k_lp_list_rows(int32_t n, const int64_t* __restrict__ rp, int32_
     if (rp[v + 1] - rp[v] > 32) rows[atomicAdd(count, 1)] = (int32_t)v;
 }
 
-// Mode of the sorted neighbour labels among eligible labels (Get_New_Label).
+// Mode of the sorted neighbour labels among eligible labels (Get_New_Label):
+// one thread per vertex of degree <= 32 (longer rows: k_lp_choose_large).
 __global__ void k_lp_choose(int32_t n, const int64_t* __restrict__ rp, const uint32_t* __restrict__ prop,
                             const int32_t* __restrict__ label, const int32_t* __restrict__ size, int32_t gmax,
                             int32_t* __restrict__ proposed, int32_t* __restrict__ join) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = rp[v], hi = rp[v + 1];
+    if (hi - lo > 32) continue;
     const int32_t own = label[v];
     int32_t best = own;
     int64_t best_cnt = 0;
-    const int64_t lo = rp[v], hi = rp[v + 1];
     int64_t i = lo;
     while (i < hi) {
       const uint32_t c = prop[i];
@@ -141,6 +143,51 @@ __global__ void k_lp_choose(int32_t n, const int64_t* __restrict__ rp, const uin
     }
     proposed[v] = best;
     if (best != own) atomicAdd(&join[best], 1);
+  }
+}
+
+// The same for the rows longer than 32 (listed in rows[0..*count)), one warp
+// per row: a lane at the end of a run gets the run's length from the previous
+// run end (a ballot within the chunk, carried across chunks); the warp keeps
+// the eligible run of largest count, the smallest label on ties - the first
+// such run in the sorted row, as the serial scan picks.
+__global__ void k_lp_choose_large(const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
+                                  const int64_t* __restrict__ rp, const uint32_t* __restrict__ prop,
+                                  const int32_t* __restrict__ label, const int32_t* __restrict__ size, int32_t gmax,
+                                  int32_t* __restrict__ proposed, int32_t* __restrict__ join) {
+  const int lane = lane_id();
+  const int64_t nrows = *count;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < nrows; r += nwarps) {
+    const int v = rows[r];
+    const int32_t own = label[v];
+    const int64_t lo = rp[v], hi = rp[v + 1];
+    unsigned long long best = 0;  // (count << 32) | (0xFFFFFFFF - label); 0 = none
+    int64_t prev_end = lo - 1;
+    for (int64_t base = lo; base < hi; base += 32) {
+      const int64_t i = base + lane;
+      const bool valid = i < hi;
+      const uint32_t c = valid ? prop[i] : 0u;
+      const bool is_end = valid && (i + 1 == hi || prop[i + 1] != c);
+      const unsigned ends = __ballot_sync(0xffffffffu, is_end);
+      if (is_end && ((int32_t)c == own || size[c] < gmax)) {
+        const unsigned below = ends & ((1u << lane) - 1u);
+        const int64_t pe = below ? base + (31 - __clz(below)) : prev_end;
+        const unsigned long long key = ((unsigned long long)(i - pe) << 32) | (0xFFFFFFFFu - c);
+        best = key > best ? key : best;
+      }
+      if (ends) prev_end = base + (31 - __clz(ends));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if (lane == 0) {
+      const int32_t b = best ? (int32_t)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFull)) : own;
+      proposed[v] = b;
+      if (b != own) atomicAdd(&join[b], 1);
+    }
   }
 }
 
@@ -280,6 +327,9 @@ int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_
       HSDL_LAUNCHED();
     }
     k_lp_choose<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, prop.p, label.p, size.p, gmax, proposed.p, join.p);
+    HSDL_LAUNCHED();
+    k_lp_choose_large<<<grid, kLpThreads, 0, st>>>(rows.p, count.p, g->rp.p, prop.p, label.p, size.p, gmax,
+                                                   proposed.p, join.p);
     HSDL_LAUNCHED();
     k_lp_apply<<<grid, kLpThreads, 0, st>>>(n, label.p, proposed.p, size.p, join.p, gmax, nlabel.p, changed.p);
     HSDL_LAUNCHED();

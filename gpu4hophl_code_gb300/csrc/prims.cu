@@ -46,20 +46,20 @@ __global__ void k_set_total(const int64_t* in, const int64_t* out, int64_t n, in
 }
 
 // ---------------------------------------------------------------------------
-// Per-row sort of (hub, hd, parent) by the 64-bit key (hub << 32 | hd).  Rows up to 32 labels: one warp per
+// Per-row sort of (key, parent) by the 64-bit label key.  Rows up to 32 labels: one warp per
 // row, bitonic network on registers.  Longer rows: one block per row, bitonic
 // network in shared memory (padded to a power of two with all-ones keys);
 // rows longer than the shared-memory capacity use a global scratch buffer.
 // ---------------------------------------------------------------------------
-__global__ void k_sort_small(int32_t n, const int64_t* __restrict__ off, uint32_t* __restrict__ hub,
-                             uint32_t* __restrict__ hd, int32_t* __restrict__ par) {
+__global__ void k_sort_small(int32_t n, const int64_t* __restrict__ off, uint64_t* __restrict__ key,
+                             int32_t* __restrict__ par) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t v = warp; v < n; v += nwarps) {
     int64_t lo = off[v], len = off[v + 1] - lo;
     if (len <= 1 || len > 32) continue;
-    uint64_t k = lane < len ? (((uint64_t)hub[lo + lane] << 32) | hd[lo + lane]) : ~0ull;
+    uint64_t k = lane < len ? key[lo + lane] : ~0ull;
     int32_t p = lane < len ? par[lo + lane] : 0;
 #pragma unroll
     for (int size = 2; size <= 32; size <<= 1) {
@@ -78,8 +78,7 @@ __global__ void k_sort_small(int32_t n, const int64_t* __restrict__ off, uint32_
       }
     }
     if (lane < len) {
-      hub[lo + lane] = (uint32_t)(k >> 32);
-      hd[lo + lane] = (uint32_t)k;
+      key[lo + lane] = k;
       par[lo + lane] = p;
     }
   }
@@ -109,8 +108,7 @@ __device__ void block_bitonic(uint64_t* sk, int32_t* sp, int P) {
 
 // rows listed in `rows` (count *nrows), each longer than 32
 __global__ void k_sort_large(const int32_t* __restrict__ rows, const int32_t* nrows, const int64_t* __restrict__ off,
-                             uint32_t* __restrict__ hub, uint32_t* __restrict__ hd, int32_t* __restrict__ par,
-                             int smem_cap,
+                             uint64_t* __restrict__ key, int32_t* __restrict__ par, int smem_cap,
                              uint64_t* __restrict__ gk, int32_t* __restrict__ gp) {
   extern __shared__ unsigned char smem_raw[];
   int cnt = *nrows;
@@ -130,13 +128,12 @@ __global__ void k_sort_large(const int32_t* __restrict__ rows, const int32_t* nr
       sp = gp;
     }
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
-      sk[i] = i < len ? (((uint64_t)hub[lo + i] << 32) | hd[lo + i]) : ~0ull;
+      sk[i] = i < len ? key[lo + i] : ~0ull;
       sp[i] = i < len ? par[lo + i] : 0;
     }
     block_bitonic(sk, sp, P);
     for (int i = threadIdx.x; i < len; i += blockDim.x) {
-      hub[lo + i] = (uint32_t)(sk[i] >> 32);
-      hd[lo + i] = (uint32_t)sk[i];
+      key[lo + i] = sk[i];
       par[lo + i] = sp[i];
     }
     __syncthreads();
@@ -178,10 +175,9 @@ int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t 
   return HSDL_OK;
 }
 
-int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int32_t* par, int64_t max_row,
-              cudaStream_t st) {
+int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int64_t max_row, cudaStream_t st) {
   int sms = device_sm_count();
-  k_sort_small<<<sms * 8, 256, 0, st>>>(n, d_off, hub, hd, par);
+  k_sort_small<<<sms * 8, 256, 0, st>>>(n, d_off, key, par);
   HSDL_LAUNCHED();
   if (max_row <= 32) return HSDL_OK;
   int32_t* rows = nullptr;
@@ -195,7 +191,7 @@ int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int3
   HSDL_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
   k_list_large_rows<<<sms * 4, 256, 0, st>>>(n, d_off, rows, count, 32, smem_cap);
   HSDL_LAUNCHED();
-  k_sort_large<<<sms * 2, 512, smem, st>>>(rows, count, d_off, hub, hd, par, smem_cap, nullptr, nullptr);
+  k_sort_large<<<sms * 2, 512, smem, st>>>(rows, count, d_off, key, par, smem_cap, nullptr, nullptr);
   HSDL_LAUNCHED();
   if (max_row > smem_cap) {
     int64_t P = 1;
@@ -208,7 +204,7 @@ int sort_rows(int32_t n, const int64_t* d_off, uint32_t* hub, uint32_t* hd, int3
     k_list_large_rows<<<sms * 4, 256, 0, st>>>(n, d_off, rows, count, smem_cap, (int32_t)max_row);
     HSDL_LAUNCHED();
     // one block walks the over-sized rows one after another through gk/gp
-    k_sort_large<<<1, 1024, smem, st>>>(rows, count, d_off, hub, hd, par, smem_cap, gk, gp);
+    k_sort_large<<<1, 1024, smem, st>>>(rows, count, d_off, key, par, smem_cap, gk, gp);
     HSDL_LAUNCHED();
     HSDL_CUDA(cudaFreeAsync(gk, st));
     HSDL_CUDA(cudaFreeAsync(gp, st));

@@ -46,8 +46,7 @@ namespace {
 
 struct IndexDesc {
   const int64_t* off;
-  const uint32_t* hub;
-  const uint32_t* hd;
+  const uint64_t* key;
   int32_t n;
   int32_t valid;
 };
@@ -169,14 +168,13 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       if (lane < cnt) r = ld_volatile_v4(ring + (mine_tk & mask));
       // every lane looks up its own request's index (and prefetches its rows
       // into L2 when the warp has several to answer)
-      IndexDesc d{nullptr, nullptr, nullptr, 0, 0};
+      IndexDesc d{nullptr, nullptr, 0, 0};
       if (lane < cnt && r.x >= 0 && r.x < max_idx) {
         d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
-        d.hub = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hub);
-        d.hd = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].hd);
+        d.key = (const uint64_t*)__ldcg((const unsigned long long*)&descs[r.x].key);
         d.n = __ldcg(&descs[r.x].n);
         d.valid = __ldcg(&descs[r.x].valid);
-        if (d.valid && cnt > Q) prefetch_rows(d.off, d.hub, d.n, r.y, r.z);
+        if (d.valid && cnt > Q) prefetch_rows(d.off, d.key, d.n, r.y, r.z);
       }
       if (lane < cnt && !d.valid) atomicAdd(&ctl->bad, 1ull);
       int32_t mine = INT_MAX;
@@ -189,10 +187,9 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         const int t = __shfl_sync(0xffffffffu, r.z, j);
         const int k = __shfl_sync(0xffffffffu, r.w, j);
         const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
-        const uint32_t* hb = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hub, j);
-        const uint32_t* hx = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.hd, j);
+        const uint64_t* kr = (const uint64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.key, j);
         const int n = __shfl_sync(0xffffffffu, d.n, j);
-        const int32_t ans = group_query<G>(active, n, off, hb, hx, s, t, k);
+        const int32_t ans = group_query<G>(active, n, off, kr, s, t, k);
         // lane j takes the answer of the group that served it
         const int src = (lane >= r0 && lane < r0 + Q) ? (lane - r0) * G : 0;
         const int32_t got = __shfl_sync(0xffffffffu, ans, src);
@@ -304,8 +301,7 @@ int write_desc(ServerImpl* S, int32_t gid, hsdl_index* idx, bool valid) {
   IndexDesc d{};
   if (idx) {
     d.off = idx->off.p;
-    d.hub = idx->hub.p;
-    d.hd = idx->hd.p;
+    d.key = idx->key.p;
     d.n = idx->n;
   }
   d.valid = valid ? 1 : 0;

@@ -309,17 +309,15 @@ class Index:
         check(lib().hsdl_extract_path(self._h, s, t, k, _ptr(e), cap, C.byref(cnt)))
         return [tuple(x) for x in e[: cnt.value].tolist()]
 
-    def set_query_tuning(self, block_threads: int = 512, prefetch_ahead: int = 0, lanes_per_query: int = 32,
-                         stage_hubs: int = 0) -> None:
-        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, lanes_per_query,
-                                stage_hubs, 0)
+    def set_query_tuning(self, block_threads: int = 512, prefetch_ahead: int = 0, lanes_per_query: int = 32) -> None:
+        t = N.hsdl_query_tuning(C.sizeof(N.hsdl_query_tuning), block_threads, prefetch_ahead, lanes_per_query)
         check(lib().hsdl_set_query_tuning(self._h, C.byref(t)))
 
     def query_tuning(self) -> dict:
         t = N.hsdl_query_tuning()
         check(lib().hsdl_get_query_tuning(self._h, C.byref(t)))
         return {"block_threads": t.block_threads, "prefetch_ahead": t.prefetch_ahead,
-                "lanes_per_query": t.lanes_per_query, "stage_hubs": t.stage_hubs}
+                "lanes_per_query": t.lanes_per_query}
 
     def save(self, path: str) -> None:
         check(lib().hsdl_save_labels(self._h, path.encode()))

@@ -208,10 +208,6 @@ typedef struct hsdl_query_tuning {
   int32_t block_threads;
   int32_t prefetch_ahead;
   int32_t lanes_per_query;
-  int32_t stage_hubs; /* > 0: each warp copies both rows' hub ids into this many words of shared memory
-                         and joins there (pairs of rows longer than that join in global memory);
-                         0: join in global memory.  Staging uses 32 lanes per query. */
-  int32_t reserved;
 } hsdl_query_tuning;
 int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* tuning);
 int hsdl_get_query_tuning(hsdl_index* idx, hsdl_query_tuning* tuning);

@@ -218,13 +218,12 @@ def test_reference_shaped_api(orc):
     assert np.array_equal(ans, orc.query(ref, q[:, 0], q[:, 1], q[:, 2]))
 
 
-@pytest.mark.parametrize("tuning", [dict(block_threads=256, stage_hubs=2048), dict(block_threads=128, stage_hubs=64),
+@pytest.mark.parametrize("tuning", [dict(block_threads=128), dict(block_threads=1024, prefetch_ahead=2),
                                     dict(block_threads=512, lanes_per_query=16), dict(block_threads=256,
                                                                                       lanes_per_query=8)])
 def test_query_variants_agree(orc, tuning):
-    """Every query kernel variant (shared-memory staging, including pairs of
-    rows too long for the buffer; 8/16/32 lanes per query) gives the same
-    answers as the oracle."""
+    """Every query kernel variant (block sizes, L2 prefetch of later rows,
+    8/16/32 lanes per query) gives the same answers as the oracle."""
     g = H.HostGraph.chung_lu(6000, 8, 2.2, 600, 1, 100, seed=26)
     K = 5
     dev, idx = gpu_build(g, K)
@@ -237,4 +236,4 @@ def test_query_variants_agree(orc, tuning):
     assert np.array_equal(base, orc.query(orc.build(g, K, threads=4), s, t, k, threads=4))
     idx.set_query_tuning(**tuning)
     assert np.array_equal(idx.query(s, t, k), base)
-    assert idx.query_tuning()["stage_hubs"] == tuning.get("stage_hubs", 0)
+    assert idx.query_tuning()["block_threads"] == tuning["block_threads"]
