@@ -18,6 +18,7 @@
 // union's rows into per-graph indexes with ids mapped back to each graph's own.
 #include <algorithm>
 #include <cmath>
+#include <deque>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -59,8 +60,11 @@ __global__ void k_split(int64_t nu, const int64_t* __restrict__ uoff, const uint
 // without hubs, capped by n (K + 1); 16 bytes per label with generation slack.
 int64_t batch_estimate_bytes(int32_t n, int64_t m2, int32_t K) {
   double avg = n ? (double)m2 / n : 0.0;
-  double pv = std::max(0.53 * std::sqrt((double)n) * std::max(0.25, avg / 10.0) * (K / 5.0),
-                       2.0 * std::pow(std::max(1.0, avg), K / 2.0));
+  // twice the power-law rule of thumb: on the 4,096-graph ER/BA batch the
+  // rule alone predicted 1.62 G labels for the first 1,024 graphs, which had
+  // 3.34 G (a build peak of 31 B per label against the 48 B allowed here)
+  double pv = 2.0 * std::max(0.53 * std::sqrt((double)n) * std::max(0.25, avg / 10.0) * (K / 5.0),
+                             2.0 * std::pow(std::max(1.0, avg), K / 2.0));
   pv = std::min(pv, (double)n * (K + 1));
   return (int64_t)(48.0 * std::max(1.0, pv) * n) + 64 * (int64_t)n + 16 * m2;
 }
@@ -253,6 +257,12 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
       x->t_gen = uidx->t_gen;
       x->t_sort = uidx->t_sort;
       x->t_clean = uidx->t_clean;
+      // the sub-batch's build, shared by its graphs
+      x->build_peak = uidx->build_peak;
+      x->build_pool = uidx->build_pool;
+      x->build_max_cand = uidx->build_max_cand;
+      x->wave_splits = uidx->wave_splits;
+      x->pool_chunks = uidx->pool_chunks;
       int64_t mr = 0;
       for (int32_t r = 0; r < gi.n; r++) mr = std::max(mr, goff[pos][r + 1] - goff[pos][r]);
       x->max_row = mr;
@@ -310,34 +320,53 @@ extern "C" int hsdl_build_batched(int32_t num_graphs, const int32_t* n, const in
     G[i] = GraphIn{n[i], row_ptr[i], col[i], w[i], K[i]};
     est[i] = batch_estimate_bytes(n[i], row_ptr[i][n[i]], K[i]);
   }
-  size_t free_b = 0, total_b = 0;
-  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
-    set_error("cudaMemGetInfo failed");
-    return HSDL_ERR_CUDA;
-  }
-  const int64_t budget = o.device_budget_bytes > 0 ? o.device_budget_bytes : (int64_t)(free_b * 0.5);
-  // greedy sub-batches in input order under the budget (and 2^28 vertices)
-  std::vector<std::vector<int32_t>> batches(1);
-  int64_t acc = 0, accn = 0;
-  for (int32_t i = 0; i < num_graphs; i++) {
-    if (!batches.back().empty() && (acc + est[i] > budget || accn + n[i] > (int64_t)(kIdMask / 2))) {
-      batches.emplace_back();
-      acc = accn = 0;
-    }
-    batches.back().push_back(i);
-    acc += est[i];
-    accn += n[i];
-  }
-  for (auto& b : batches) {
-    int rc = build_sub_batch(G, b, o, out);
-    if (rc != HSDL_OK) {
-      for (int32_t i = 0; i < num_graphs; i++)
-        if (out[i]) {
-          free_index_handle(out[i]);
-          out[i] = nullptr;
+  // Sub-batches are formed as the build goes, in input order: each takes
+  // graphs while their estimated bytes fit in the budget - the given one, or
+  // 45 % of the HBM free at that moment (the indexes of earlier sub-batches
+  // stay resident) - and under 2^27 vertices.  A sub-batch that runs out of
+  // memory all the same is built again as two halves.
+  auto fail = [&](int rc) {
+    for (int32_t i = 0; i < num_graphs; i++)
+      if (out[i]) {
+        free_index_handle(out[i]);
+        out[i] = nullptr;
+      }
+    return rc;
+  };
+  std::deque<std::vector<int32_t>> retry;
+  int32_t next = 0;
+  while (next < num_graphs || !retry.empty()) {
+    std::vector<int32_t> b;
+    if (!retry.empty()) {
+      b = std::move(retry.front());
+      retry.pop_front();
+    } else {
+      int64_t budget = o.device_budget_bytes;
+      if (budget <= 0) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+          set_error("cudaMemGetInfo failed");
+          return fail(HSDL_ERR_CUDA);
         }
-      return rc;
+        budget = (int64_t)(free_b * 0.45);
+      }
+      int64_t acc = 0, accn = 0;
+      while (next < num_graphs &&
+             (b.empty() || (acc + est[next] <= budget && accn + n[next] <= (int64_t)(kIdMask / 2)))) {
+        acc += est[next];
+        accn += n[next];
+        b.push_back(next++);
+      }
     }
+    const int rc = build_sub_batch(G, b, o, out);
+    if (rc == HSDL_ERR_NOMEM && b.size() > 1) {
+      cudaGetLastError();  // the failed allocation is not sticky; clear it
+      const size_t h = b.size() / 2;
+      retry.emplace_front(b.begin() + (std::ptrdiff_t)h, b.end());
+      retry.emplace_front(b.begin(), b.begin() + (std::ptrdiff_t)h);
+      continue;
+    }
+    if (rc != HSDL_OK) return fail(rc);
   }
   return HSDL_OK;
 }

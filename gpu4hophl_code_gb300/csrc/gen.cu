@@ -27,10 +27,10 @@
 //    which the clean reduces exactly to the canonical set.  Waves start at one
 //    hub and double, so the highest-ranked hubs - which produce most labels
 //    and prune the most - are seen by nearly everyone.
-//  * Committed labels live in a pool of per-vertex rows with slack capacity
-//    (bump allocation, rows double when they overflow), so a commit only
-//    touches the rows that receive labels.  The final index is compacted to
-//    exact CSR and each row sorted by label key.
+//  * Committed labels live in a pool of per-vertex rows made of doubling
+//    segments (nothing is moved when a row grows), so a commit only touches
+//    the rows that receive labels.  The final index is compacted to exact CSR
+//    and each row sorted by label key.
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -362,18 +362,36 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
     const int64_t i0 = c0 + (int64_t)took;
     if (i0 >= c1) break;
     const int64_t i1 = min(c1, i0 + 8 * NG);
-    for (int64_t i = i0 + gi; i < i1; i += NG) {
-      int2 e = C[i];
-      int slot = e.x, v = e.y;
-      uint64_t ck = cand[map.row(slot) + map.local(v)];
+    // The group's (up to) 8 candidates i0 + gi + NG c: lane c loads candidate
+    // c's entry, key, table and row length up front, so the 8 candidates cost
+    // two rounds of memory latency before their scans instead of two each.
+    int2 pe = make_int2(0, 0);
+    uint64_t pck = 0;
+    int pcap = 0, plen = 0;
+    int64_t ptoff = 0;
+    {
+      const int64_t mi = i0 + gi + (int64_t)NG * gl;
+      if (gl < 8 && mi < i1) {
+        pe = C[mi];
+        pck = cand[map.row(pe.x) + map.local(pe.y)];
+        pcap = tab_cap[pe.x];
+        ptoff = tab_off[pe.x];
+        plen = row_len[pe.y];
+      }
+    }
+    for (int c = 0; c < 8; c++) {
+      if (i0 + gi + (int64_t)NG * c >= i1) break;  // uniform over the group
+      const int slot = __shfl_sync(gmask, pe.x, c, G), v = __shfl_sync(gmask, pe.y, c, G);
+      const uint64_t ck = __shfl_sync(gmask, (unsigned long long)pck, c, G);
+      const int cap = __shfl_sync(gmask, pcap, c, G);
+      const int64_t toff = (int64_t)__shfl_sync(gmask, (long long)ptoff, c, G);
+      const int len = __shfl_sync(gmask, plen, c, G);
       long long d = (long long)ckey_dist(ck);
       long long q = LLONG_MAX;
-      int cap = tab_cap[slot];
       if (cap > 0) {
-        const int32_t* T = tab + tab_off[slot] * stride;
+        const int32_t* T = tab + toff * stride;
         const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
         uint32_t mask = (uint32_t)cap - 1;
-        int len = row_len[v];
         // lane gl of the group holds the address of the row's segment gl, so
         // a label's address takes a shuffle instead of two dependent loads
         const uint64_t* my_seg = nullptr;
@@ -599,10 +617,11 @@ std::vector<int32_t> wave_schedule(int32_t n, int32_t first, int32_t max_wave) {
 
 int32_t auto_max_wave(int32_t n, int64_t budget_bytes) {
   // dense candidate rows: max_wave * n * 8 B within an eighth of the budget,
-  // at most 2048 hubs per wave
+  // at most 8192 hubs per wave (at n = 1M: 2048 hubs 2.26 s, 4096 2.21 s,
+  // 8192 2.16 s of generation)
   int64_t avail = budget_bytes > 0 ? budget_bytes / 8 : (int64_t)16 << 30;
   int64_t w = avail / ((int64_t)n * 8);
-  w = std::max<int64_t>(1, std::min<int64_t>(2048, w));
+  w = std::max<int64_t>(1, std::min<int64_t>(8192, w));
   return (int32_t)w;
 }
 
@@ -633,7 +652,21 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   int64_t budget = opts.device_budget_bytes > 0 ? opts.device_budget_bytes : (int64_t)free_b;
   std::vector<int32_t> bounds;
   if (plan) {
-    bounds = plan->bounds;
+    // the plan's layer waves, split where a wave's dense candidate rows would
+    // pass an eighth of the budget
+    const int64_t cand_cap = std::max<int64_t>((int64_t)1 << 20, budget / 8 / (int64_t)sizeof(uint64_t));
+    bounds.push_back(0);
+    for (size_t i = 0; i + 1 < plan->bounds.size(); i++) {
+      int64_t acc = 0;
+      for (int32_t v = plan->bounds[i]; v < plan->bounds[i + 1]; v++) {
+        if (acc > 0 && acc + plan->comp_n[v] > cand_cap) {
+          bounds.push_back(v);
+          acc = 0;
+        }
+        acc += plan->comp_n[v];
+      }
+      bounds.push_back(plan->bounds[i + 1]);
+    }
   } else {
     int32_t max_wave = opts.max_wave > 0 ? opts.max_wave : auto_max_wave(n, budget);
     bounds = wave_schedule(n, opts.first_wave > 0 ? opts.first_wave : 1, max_wave);
@@ -886,7 +919,11 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       // order generates a superset of the canonical labels).
       HSDL_CUDA(cudaMemsetAsync(cand.p, 0xFF, (size_t)wave_entries * sizeof(uint64_t), st));
       const int64_t want = std::max<int64_t>(capC * 2, (int64_t)hc.c_count * 2);
-      if (want > c_limit && W > 1) {
+      size_t fb_now = 0, tb_now = 0;
+      HSDL_CUDA(cudaMemGetInfo(&fb_now, &tb_now));
+      // the lists are replaced, not grown: the old ones are freed first
+      const int64_t list_room = ((int64_t)fb_now + capC * kListEntryBytes) / 2;
+      if ((want > c_limit || want * kListEntryBytes > list_room) && W > 1) {
         bounds.insert(bounds.begin() + (std::ptrdiff_t)wv + 1, s_hub + W / 2);
         idx->wave_splits++;
         split = true;
@@ -902,6 +939,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     }
     if (split) continue;
     idx->work_relax += (int64_t)hc.relax;
+    idx->work_candidates += (int64_t)std::min<unsigned long long>(hc.c_count, (unsigned long long)capC);
     idx->work_join_reads += (int64_t)hc.reads;
     idx->work_labels_written += (int64_t)hc.wl_count;
     // commit the wave's labels

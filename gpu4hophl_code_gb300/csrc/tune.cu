@@ -71,7 +71,7 @@ std::vector<Axis> axes_for(bool batched) {
   if (batched)
     a.push_back({&hsdl_build_opts::max_wave, {65536, 131072, 262144, 524288}});
   else
-    a.push_back({&hsdl_build_opts::max_wave, {512, 1024, 2048, 4096}});
+    a.push_back({&hsdl_build_opts::max_wave, {1024, 2048, 4096, 8192}});
   a.push_back({&hsdl_build_opts::block_threads, {128, 256, 512}});
   a.push_back({&hsdl_build_opts::frontier_tile, {0, 1024, 4096}});
   a.push_back({&hsdl_build_opts::prune_lanes, {0, 8, 16, 32}});
@@ -95,9 +95,13 @@ int hsdl_build_autotune(hsdl_graph* g, int32_t K, int32_t sample_hubs, hsdl_buil
     set_error("K * max edge weight must be < 2^28");
     return HSDL_ERR_INVALID;
   }
-  const int32_t limit = sample_hubs > 0 ? std::min(sample_hubs, g->n) : std::min<int32_t>(g->n, 16384);
+  // default sample: the whole generation up to 2M vertices (a prefix of hubs
+  // misjudges the wave width: at n = 1M the first 16,384 hubs favoured 1024
+  // hubs per wave, the whole build 8192), else the first 262,144 hubs
+  const int32_t limit =
+      sample_hubs > 0 ? std::min(sample_hubs, g->n) : (g->n <= 2000000 ? g->n : std::min<int32_t>(g->n, 262144));
   hsdl_build_opts best = *opts;
-  if (best.max_wave == 0) best.max_wave = 2048;
+  if (best.max_wave == 0) best.max_wave = 4096;
   if (best.block_threads == 0) best.block_threads = 256;
   auto trial = [&](const hsdl_build_opts& c, int* rc) -> double {
     hsdl_index* idx = nullptr;

@@ -134,8 +134,10 @@ int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index
  * row_ptr[i], col[i], w[i]) with hop bound K[i]; out[i] receives its index,
  * bit-identical to hsdl_build of that graph alone.  The graphs run as one
  * disjoint union whose waves hold the same ranks of many graphs together;
- * graphs are grouped into sub-batches whose estimated labels fit
- * opts->device_budget_bytes (0 = half of free HBM).  A batched wave holds at
+ * graphs are grouped, in input order, into sub-batches whose estimated build
+ * bytes fit opts->device_budget_bytes (0 = 45% of the HBM free when the
+ * sub-batch starts; the indexes already built stay resident), and a
+ * sub-batch that runs out of memory is built again as two halves.  A batched wave holds at
  * most 64 rank layers and opts->max_wave hubs (0 = 262144).  No counterpart
  * in the reference, which builds one graph per run. */
 int hsdl_build_batched(int32_t num_graphs, const int32_t* n, const int64_t* const* row_ptr,
@@ -144,8 +146,9 @@ int hsdl_build_batched(int32_t num_graphs, const int32_t* n, const int64_t* cons
 
 /* Autotuning of the launch shapes above (block_threads, frontier_tile,
  * prune_lanes, max_wave); the labels never depend on them.  Times the
- * generation of the graph's first sample_hubs hubs (0 = 16384), the
- * highest-ranked and widest searches, under candidate settings by coordinate
+ * generation of the graph's first sample_hubs hubs (0 = all of them up to 2M
+ * vertices, else 262144), the highest-ranked and widest searches first,
+ * under candidate settings by coordinate
  * descent, and writes the fastest into *opts (its other fields are kept).
  * best_seconds and trials (either may be NULL) receive the fastest sample
  * time and the number of timed runs.  No counterpart in the reference, whose
@@ -239,6 +242,7 @@ typedef struct hsdl_index_info {
   int64_t work_join_reads;       /* committed labels read by the pruning joins */
   int64_t work_labels_written;   /* labels generated (before clean) */
   int64_t work_clean_reads;      /* labels read by the clean's joins */
+  int64_t work_candidates;       /* (hub, vertex) candidates the pruning joins decided */
   /* device memory of the build */
   int64_t build_peak_bytes;      /* most HBM the build's buffers held at once */
   int64_t build_pool_entries;    /* label-pool entries the generation's rows occupied (labels and row slack) */

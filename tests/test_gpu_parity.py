@@ -74,7 +74,7 @@ def test_autotune_picks_valid_shapes():
     dev = H.Graph(g)
     r = H.autotune_build(dev, 5, sample_hubs=4096)
     assert r["block_threads"] in (128, 256, 512) and r["prune_lanes"] in (0, 8, 16, 32)
-    assert r["max_wave"] in (512, 1024, 2048, 4096) and r["frontier_tile"] >= 0
+    assert r["max_wave"] in (1024, 2048, 4096, 8192) and r["frontier_tile"] >= 0
     assert r["seconds"] > 0 and r["trials"] >= 10
     shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
     a = H.Index.build(dev, 5, **shapes).export()
