@@ -451,7 +451,7 @@ def run_batched(args, dist, rank, world, local):
     t0 = time.perf_counter()
     tuned = H.autotune_build_batched(graphs, Ks, sample_graphs=256)
     tune_s = time.perf_counter() - t0
-    shapes = {k: tuned[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    shapes = {k: tuned[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes", "prune_pairs")}
     for _ in range(args.warmup):
         for ix in H.Index.build_batched(graphs[:64], Ks[:64], **shapes):
             ix.close()

@@ -382,6 +382,7 @@ static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
   HSDL_CHECK_ARG(o->frontier_tile >= 0, "frontier_tile must be >= 0");
   HSDL_CHECK_ARG(o->prune_lanes == 0 || o->prune_lanes == 8 || o->prune_lanes == 16 || o->prune_lanes == 32,
                  "prune_lanes must be 0, 8, 16 or 32");
+  HSDL_CHECK_ARG(o->prune_pairs >= 0 && o->prune_pairs <= 2, "prune_pairs must be 0, 1 or 2");
   return HSDL_OK;
 }
 
@@ -445,21 +446,29 @@ int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_
   HSDL_CHECK_ARG(idx && nq >= 0, "bad arguments");
   if (nq == 0) return HSDL_OK;
   HSDL_CHECK_ARG(s && t && k && out, "null query array");
-  for (int64_t i = 0; i < nq; i++)
-    HSDL_CHECK_ARG(s[i] >= 0 && s[i] < idx->n && t[i] >= 0 && t[i] < idx->n,
-                   "query vertex out of range at query " + std::to_string(i));
   cudaStream_t st = idx->stream;
+  // queries, answers and the id check's result in one allocation; the ids
+  // are checked on the device (a host loop over 10M queries cost a quarter of
+  // the call), and a batch naming a vertex outside the index is an error
   int32_t* d = nullptr;
-  HSDL_CUDA(cudaMallocAsync(&d, sizeof(int32_t) * 4 * nq, st));
+  HSDL_CUDA(cudaMallocAsync(&d, sizeof(int32_t) * 4 * nq + sizeof(unsigned long long), st));
+  unsigned long long* d_first = (unsigned long long*)(d + 4 * nq);
   HSDL_CUDA(cudaMemcpyAsync(d, s, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
   HSDL_CUDA(cudaMemcpyAsync(d + nq, t, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
   HSDL_CUDA(cudaMemcpyAsync(d + 2 * nq, k, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
-  int rc = query_device(idx, nq, d, d + nq, d + 2 * nq, d + 3 * nq, st);
+  int rc = first_bad_query(idx, nq, d, d + nq, d_first, st);
+  if (rc == HSDL_OK) rc = query_device(idx, nq, d, d + nq, d + 2 * nq, d + 3 * nq, st);
+  unsigned long long first = ~0ull;
   if (rc == HSDL_OK) {
     HSDL_CUDA(cudaMemcpyAsync(out, d + 3 * nq, sizeof(int32_t) * nq, cudaMemcpyDeviceToHost, st));
+    HSDL_CUDA(cudaMemcpyAsync(&first, d_first, sizeof(first), cudaMemcpyDeviceToHost, st));
   }
   HSDL_CUDA(cudaFreeAsync(d, st));
   HSDL_CUDA(cudaStreamSynchronize(st));
+  if (rc == HSDL_OK && first != ~0ull) {
+    set_error("query vertex out of range at query " + std::to_string(first));
+    return HSDL_ERR_INVALID;
+  }
   if (rc == HSDL_OK) rc = query_error(idx);
   return rc;
 }

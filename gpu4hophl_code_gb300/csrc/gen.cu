@@ -337,7 +337,7 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 // read G labels of v at a time and stop as soon as one dominates.  Warps take
 // 8 candidates per group at a time from a per-hop counter, so candidates with
 // long label lists do not hold back a statically assigned share.
-template <int G>
+template <int G, int P>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
                                                     Rows rows, const int32_t* __restrict__ row_len,
@@ -439,22 +439,27 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
             ix = (ix + 1) & mask;
           }
         };
-        uint64_t a0, a1;
-        load_pair(2 * gl, a0, a1);
-        for (int j0 = 0; j0 < len; j0 += 2 * G) {
-          uint64_t b0, b1;
-          load_pair(j0 + 2 * G + 2 * gl, b0, b1);
-          const bool c0 = (int)lkey_hop(a0) <= h, c1 = (int)lkey_hop(a1) <= h;
-          const uint32_t fb0 = filter_bit<kSlotFilterBits>(lkey_hub(a0));
-          const uint32_t fb1 = filter_bit<kSlotFilterBits>(lkey_hub(a1));
-          const uint32_t f0 = c0 ? __ldg(Fl + (fb0 >> 5)) : 0u;
-          const uint32_t f1 = c1 ? __ldg(Fl + (fb1 >> 5)) : 0u;
-          if (c0) probe(a0, f0);
-          if (c1) probe(a1, f1);
-          scanned += (unsigned long long)min(2 * G, len - j0);
+        // a step covers 2 P G labels: lane gl takes the pairs at 2 gl + 2 G p
+        uint64_t a[2 * P];
+#pragma unroll
+        for (int p = 0; p < P; p++) load_pair(2 * gl + 2 * G * p, a[2 * p], a[2 * p + 1]);
+        for (int j0 = 0; j0 < len; j0 += 2 * G * P) {
+          uint64_t b[2 * P];
+#pragma unroll
+          for (int p = 0; p < P; p++) load_pair(j0 + 2 * G * P + 2 * gl + 2 * G * p, b[2 * p], b[2 * p + 1]);
+          uint32_t f[2 * P];
+#pragma unroll
+          for (int x = 0; x < 2 * P; x++) {
+            const uint32_t fb = filter_bit<kSlotFilterBits>(lkey_hub(a[x]));
+            f[x] = (int)lkey_hop(a[x]) <= h ? __ldg(Fl + (fb >> 5)) : 0u;
+          }
+#pragma unroll
+          for (int x = 0; x < 2 * P; x++)
+            if ((int)lkey_hop(a[x]) <= h) probe(a[x], f[x]);
+          scanned += (unsigned long long)min(2 * G * P, len - j0);
           if (__any_sync(gmask, q <= d)) break;  // already dominated
-          a0 = b0;
-          a1 = b1;
+#pragma unroll
+          for (int x = 0; x < 2 * P; x++) a[x] = b[x];
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) {
@@ -810,9 +815,13 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   const int g_expand = sms * (tpb == 128   ? resident_blocks(k_expand<128>, 128)
                               : tpb == 512 ? resident_blocks(k_expand<512>, 512)
                                            : resident_blocks(k_expand<256>, 256));
-  const int g_prune8 = sms * resident_blocks(k_prune<8>, kThreads);
-  const int g_prune16 = sms * resident_blocks(k_prune<16>, kThreads);
-  const int g_prune32 = sms * resident_blocks(k_prune<32>, kThreads);
+  const int pairs = opts.prune_pairs == 2 ? 2 : 1;
+  const int g_prune8 = sms * (pairs == 2 ? resident_blocks(k_prune<8, 2>, kThreads)
+                                         : resident_blocks(k_prune<8, 1>, kThreads));
+  const int g_prune16 = sms * (pairs == 2 ? resident_blocks(k_prune<16, 2>, kThreads)
+                                          : resident_blocks(k_prune<16, 1>, kThreads));
+  const int g_prune32 = sms * (pairs == 2 ? resident_blocks(k_prune<32, 2>, kThreads)
+                                          : resident_blocks(k_prune<32, 1>, kThreads));
   int lanes = 32;
 
   Counters hc;
@@ -844,12 +853,19 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_CUDA(cudaGetLastError());
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());
-#define HSDL_PRUNE(G, GRID)                                                                                  \
-  k_prune<G><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,                 \
-                                        tab_cap.p, tab.p, stride, filt.p, Fout, wl_v.p, wl_key.p, wl_par.p, ctr.p)
-      if (lanes == 8) HSDL_PRUNE(8, g_prune8);
-      else if (lanes == 16) HSDL_PRUNE(16, g_prune16);
-      else HSDL_PRUNE(32, g_prune32);
+#define HSDL_PRUNE(G, P, GRID)                                                                              \
+  k_prune<G, P><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,             \
+                                           tab_cap.p, tab.p, stride, filt.p, Fout, wl_v.p, wl_key.p, wl_par.p, \
+                                           ctr.p)
+      if (pairs == 2) {
+        if (lanes == 8) HSDL_PRUNE(8, 2, g_prune8);
+        else if (lanes == 16) HSDL_PRUNE(16, 2, g_prune16);
+        else HSDL_PRUNE(32, 2, g_prune32);
+      } else {
+        if (lanes == 8) HSDL_PRUNE(8, 1, g_prune8);
+        else if (lanes == 16) HSDL_PRUNE(16, 1, g_prune16);
+        else HSDL_PRUNE(32, 1, g_prune32);
+      }
 #undef HSDL_PRUNE
       HSDL_CUDA(cudaGetLastError());
     }

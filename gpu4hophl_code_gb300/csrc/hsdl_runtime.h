@@ -157,6 +157,10 @@ int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_
              int32_t* iterations_run);
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st);
+// Device check of a query batch's vertex ids: *d_first (device) becomes the
+// smallest index of a query with s or t outside [0, n), all-ones if none.
+int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, unsigned long long* d_first,
+                    cudaStream_t st);
 int query_error(hsdl_index_impl* idx);  // HSDL_ERR_TIMEOUT (and clears) if a query kernel flagged one
 int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int64_t max_row, cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total

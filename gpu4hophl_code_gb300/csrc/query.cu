@@ -63,7 +63,26 @@ int launch_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
   return HSDL_OK;
 }
 
+// Smallest index of a query naming a vertex outside [0, n) (stays all-ones if none).
+__global__ void k_first_bad_id(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
+                               unsigned long long* first) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += (int64_t)gridDim.x * blockDim.x) {
+    const int s = qs[i], t = qt[i];
+    if (s < 0 || s >= n || t < 0 || t >= n) atomicMin(first, (unsigned long long)i);
+  }
+}
+
 }  // namespace
+
+int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, unsigned long long* d_first,
+                    cudaStream_t st) {
+  HSDL_CUDA(cudaMemsetAsync(d_first, 0xFF, sizeof(unsigned long long), st));
+  if (nq <= 0) return HSDL_OK;
+  const int sms = device_sm_count();
+  k_first_bad_id<<<sms * 4, 256, 0, st>>>(idx->n, nq, s, t, d_first);
+  HSDL_LAUNCHED();
+  return HSDL_OK;
+}
 
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st) {

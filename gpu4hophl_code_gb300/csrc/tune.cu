@@ -75,6 +75,7 @@ std::vector<Axis> axes_for(bool batched) {
   a.push_back({&hsdl_build_opts::block_threads, {128, 256, 512}});
   a.push_back({&hsdl_build_opts::frontier_tile, {0, 1024, 4096}});
   a.push_back({&hsdl_build_opts::prune_lanes, {0, 8, 16, 32}});
+  a.push_back({&hsdl_build_opts::prune_pairs, {1, 2}});
   return a;
 }
 

@@ -169,7 +169,8 @@ def generate_Group_CDLP(instance_graph, groups: list, MAX_GROUP_SIZE: int, max_i
 
 
 def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block_threads: int = 0,
-               frontier_tile: int = 0, prune_lanes: int = 0, device_budget_bytes: int = 0) -> N.hsdl_build_opts:
+               frontier_tile: int = 0, prune_lanes: int = 0, prune_pairs: int = 0,
+               device_budget_bytes: int = 0) -> N.hsdl_build_opts:
     o = N.hsdl_build_opts()
     lib().hsdl_build_opts_default(C.byref(o))
     o.clean = int(clean)
@@ -178,11 +179,12 @@ def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block
     o.block_threads = block_threads
     o.frontier_tile = frontier_tile
     o.prune_lanes = prune_lanes
+    o.prune_pairs = prune_pairs
     o.device_budget_bytes = device_budget_bytes
     return o
 
 
-_TUNABLES = ("max_wave", "block_threads", "frontier_tile", "prune_lanes")
+_TUNABLES = ("max_wave", "block_threads", "frontier_tile", "prune_lanes", "prune_pairs")
 
 
 def autotune_build(graph: "Graph", K: int, sample_hubs: int = 0, **opts) -> dict:

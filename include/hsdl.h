@@ -118,7 +118,7 @@ typedef struct hsdl_build_opts {
   int32_t block_threads;  /* threads per expansion block: 128, 256 or 512 (0 = 256) */
   int32_t frontier_tile;  /* frontier entries an expansion block takes at a time (0 = one block's worth) */
   int32_t prune_lanes;    /* lanes per candidate in the pruning join: 8, 16 or 32 (0 = per wave, by mean row length) */
-  int32_t reserved;
+  int32_t prune_pairs;    /* label pairs each lane of the pruning join loads per step: 1 or 2 (0 = 1) */
   int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
 } hsdl_build_opts;
 

@@ -75,7 +75,7 @@ def test_batched_autotune_and_small_waves():
     r = H.autotune_build_batched(graphs, Ks, sample_graphs=8)
     assert r["block_threads"] in (128, 256, 512) and r["prune_lanes"] in (0, 8, 16, 32)
     assert r["max_wave"] in (65536, 131072, 262144, 524288) and r["trials"] >= 10
-    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes", "prune_pairs")}
     tuned = H.Index.build_batched(graphs, Ks, **shapes)
     small = H.Index.build_batched(graphs, Ks, max_wave=256, prune_lanes=8)
     for g, K, a, b in zip(graphs, Ks, tuned, small):

@@ -55,15 +55,15 @@ def test_uncleaned_generation_matches_wave_oracle(orc, max_wave):
     assert np.array_equal(off2, canon.off) and np.array_equal(lab2, canon.lab)
 
 
-@pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes", [(128, 0, 8), (512, 4096, 16), (256, 1024, 32),
-                                                                     (256, 0, 0)])
-def test_launch_shapes_do_not_change_labels(orc, block_threads, frontier_tile, prune_lanes):
+@pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes,prune_pairs",
+                         [(128, 0, 8, 1), (512, 4096, 16, 2), (256, 1024, 32, 1), (256, 0, 0, 2), (256, 0, 8, 2)])
+def test_launch_shapes_do_not_change_labels(orc, block_threads, frontier_tile, prune_lanes, prune_pairs):
     """The uncleaned superset depends on the wave schedule only; threads per
     block, frontier tile and prune lanes change the time, never a label."""
     g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=22)
     K = 5
     dev, idx = gpu_build(g, K, clean=False, max_wave=64, block_threads=block_threads,
-                         frontier_tile=frontier_tile, prune_lanes=prune_lanes)
+                         frontier_tile=frontier_tile, prune_lanes=prune_lanes, prune_pairs=prune_pairs)
     off, lab = idx.export()
     ref = orc.build(g, K, threads=4, wave_bounds=H.wave_bounds(g.n, max_wave=64), clean=False)
     assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
@@ -76,7 +76,7 @@ def test_autotune_picks_valid_shapes():
     assert r["block_threads"] in (128, 256, 512) and r["prune_lanes"] in (0, 8, 16, 32)
     assert r["max_wave"] in (1024, 2048, 4096, 8192) and r["frontier_tile"] >= 0
     assert r["seconds"] > 0 and r["trials"] >= 10
-    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes")}
+    shapes = {k: r[k] for k in ("max_wave", "block_threads", "frontier_tile", "prune_lanes", "prune_pairs")}
     a = H.Index.build(dev, 5, **shapes).export()
     b = H.Index.build(dev, 5).export()
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
@@ -237,3 +237,22 @@ def test_query_variants_agree(orc, tuning):
     idx.set_query_tuning(**tuning)
     assert np.array_equal(idx.query(s, t, k), base)
     assert idx.query_tuning()["block_threads"] == tuning["block_threads"]
+
+
+def test_query_batch_rejects_vertices_outside_the_index():
+    """hsdl_query_batch checks the vertex ids of a batch (on the device) and
+    names the first query that is out of range."""
+    g = H.HostGraph.erdos_renyi(500, 2000, 1, 50, seed=27)
+    dev, idx = gpu_build(g, 4)
+    s = np.arange(1000, dtype=np.int32) % g.n
+    t = (np.arange(1000, dtype=np.int32) * 7) % g.n
+    k = np.full(1000, 3, np.int32)
+    ok = idx.query(s, t, k)
+    assert ok.shape == (1000,)
+    for bad_s, bad_t, at in ((g.n, 0, 417), (3, -1, 12), (-5, g.n + 9, 998)):
+        s2, t2 = s.copy(), t.copy()
+        s2[at], t2[at] = bad_s, bad_t
+        with pytest.raises(H.HsdlError) as e:
+            idx.query(s2, t2, k)
+        assert f"at query {at}" in str(e.value)
+    assert np.array_equal(idx.query(s, t, k), ok)  # the index is unaffected
