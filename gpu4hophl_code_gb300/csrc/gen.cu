@@ -362,36 +362,21 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
     const int64_t i0 = c0 + (int64_t)took;
     if (i0 >= c1) break;
     const int64_t i1 = min(c1, i0 + 8 * NG);
-    // The group's (up to) 8 candidates i0 + gi + NG c: lane c loads candidate
-    // c's entry, key, table and row length up front, so the 8 candidates cost
-    // two rounds of memory latency before their scans instead of two each.
-    int2 pe = make_int2(0, 0);
-    uint64_t pck = 0;
-    int pcap = 0, plen = 0;
-    int64_t ptoff = 0;
-    {
-      const int64_t mi = i0 + gi + (int64_t)NG * gl;
-      if (gl < 8 && mi < i1) {
-        pe = C[mi];
-        pck = cand[map.row(pe.x) + map.local(pe.y)];
-        pcap = tab_cap[pe.x];
-        ptoff = tab_off[pe.x];
-        plen = row_len[pe.y];
-      }
-    }
-    for (int c = 0; c < 8; c++) {
-      if (i0 + gi + (int64_t)NG * c >= i1) break;  // uniform over the group
-      const int slot = __shfl_sync(gmask, pe.x, c, G), v = __shfl_sync(gmask, pe.y, c, G);
-      const uint64_t ck = __shfl_sync(gmask, (unsigned long long)pck, c, G);
-      const int cap = __shfl_sync(gmask, pcap, c, G);
-      const int64_t toff = (int64_t)__shfl_sync(gmask, (long long)ptoff, c, G);
-      const int len = __shfl_sync(gmask, plen, c, G);
+    // (Loading the set-up of a group's 8 candidates up front, one lane each,
+    // doubled the registers of the 32-lane kernel and halved its occupancy:
+    // generation went from 2.28 s to 2.83 s at n = 1M.)
+    for (int64_t i = i0 + gi; i < i1; i += NG) {
+      int2 e = C[i];
+      int slot = e.x, v = e.y;
+      uint64_t ck = cand[map.row(slot) + map.local(v)];
       long long d = (long long)ckey_dist(ck);
       long long q = LLONG_MAX;
+      int cap = tab_cap[slot];
       if (cap > 0) {
-        const int32_t* T = tab + toff * stride;
+        const int32_t* T = tab + tab_off[slot] * stride;
         const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
         uint32_t mask = (uint32_t)cap - 1;
+        int len = row_len[v];
         // lane gl of the group holds the address of the row's segment gl, so
         // a label's address takes a shuffle instead of two dependent loads
         const uint64_t* my_seg = nullptr;
