@@ -154,10 +154,11 @@ struct SlotMap {
 // wave set-up
 // ---------------------------------------------------------------------------
 __global__ void k_wave_init(int32_t W, int32_t s_hub, SlotMap map, uint64_t* __restrict__ cand, int2* __restrict__ C,
-                            int4* __restrict__ F, Counters* ctr) {
+                            int4* __restrict__ F, Counters* ctr, int32_t* __restrict__ wave_end_of) {
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot < W) {
     int hub = s_hub + slot;
+    wave_end_of[hub] = s_hub + W;
     cand[map.row(slot) + map.local(hub)] = ckey(0, 0, (uint32_t)hub);
     C[slot] = make_int2(slot, hub);
     F[slot] = make_int4(slot, hub, 0, 0);
@@ -196,9 +197,13 @@ __global__ void k_table_size(int32_t W, int32_t s_hub, const int32_t* __restrict
 }
 
 // Inserts every label (w, hop, d) of the hub into its table: T[w][hop] = min d.
+// Also records, per slot, the end of the wave of the hub's highest hub id
+// (tab_theta): labels of a vertex at or past it come from later waves, whose
+// hubs the wave's hub has no label for, so the pruning join stops there.
 __global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t* __restrict__ row_len,
                              const int64_t* __restrict__ tab_off, const int32_t* __restrict__ tab_cap,
-                             int32_t* __restrict__ tab, int stride, uint32_t* __restrict__ filt) {
+                             int32_t* __restrict__ tab, int stride, uint32_t* __restrict__ filt,
+                             const int32_t* __restrict__ wave_end_of, int32_t* __restrict__ tab_theta) {
   int lane = lane_id();
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -209,9 +214,11 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t*
     int32_t* T = tab + tab_off[slot] * stride;
     uint32_t mask = (uint32_t)cap - 1;
     int len = row_len[hub];
+    int32_t wmax = 0;
     for (int j = lane; j < len; j += 32) {
       uint64_t k = rows.key(hub, j);
       int32_t w = (int32_t)lkey_hub(k);
+      wmax = max(wmax, w);
       const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
       atomicOr(&filt[slot * kSlotFilterWords + (fb >> 5)], 1u << (fb & 31));
       uint32_t i = table_hash((uint32_t)w, mask);
@@ -226,6 +233,9 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t*
       }
       if (placed) atomicMin(&T[(int64_t)i * stride + 1 + lkey_hop(k)], (int32_t)lkey_dist(k));
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if (lane == 0) tab_theta[slot] = wave_end_of[wmax];
   }
 }
 
@@ -345,6 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
                                                     const int32_t* __restrict__ tab_cap,
                                                     const int32_t* __restrict__ tab, int stride,
                                                     const uint32_t* __restrict__ filt,
+                                                    const int32_t* __restrict__ tab_theta,
                                                     int4* __restrict__ Fout, int32_t* __restrict__ wl_v,
                                                     uint64_t* __restrict__ wl_key, int32_t* __restrict__ wl_par,
                                                     Counters* ctr) {
@@ -375,6 +386,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
       if (cap > 0) {
         const int32_t* T = tab + tab_off[slot] * stride;
         const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
+        const uint32_t theta = (uint32_t)tab_theta[slot];
         uint32_t mask = (uint32_t)cap - 1;
         int len = row_len[v];
         // lane gl of the group holds the address of the row's segment gl, so
@@ -438,11 +450,14 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
             const uint32_t fb = filter_bit<kSlotFilterBits>(lkey_hub(a[x]));
             f[x] = (int)lkey_hop(a[x]) <= h ? __ldg(Fl + (fb >> 5)) : 0u;
           }
+          bool past = false;  // a label from a wave after the hub's last hub: the rest of the row is too
 #pragma unroll
-          for (int x = 0; x < 2 * P; x++)
+          for (int x = 0; x < 2 * P; x++) {
             if ((int)lkey_hop(a[x]) <= h) probe(a[x], f[x]);
+            past |= lkey_hub(a[x]) >= theta;
+          }
           scanned += (unsigned long long)min(2 * G * P, len - j0);
-          if (__any_sync(gmask, q <= d)) break;  // already dominated
+          if (__any_sync(gmask, q <= d || past)) break;  // dominated, or nothing further can match
 #pragma unroll
           for (int x = 0; x < 2 * P; x++) a[x] = b[x];
         }
@@ -702,6 +717,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<int64_t> tab_off;
   DevBuf<int32_t> tab_cap, tab;
   DevBuf<uint32_t> filt;
+  DevBuf<int32_t> wave_end_of, tab_theta;  // end of each started hub's wave; per-slot stop threshold
   DevBuf<Counters> ctr;
   auto release_pool = [&]() {
     for (auto& c : chunk_keys) c.release();
@@ -714,7 +730,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     cand.release(); row_len.release(); cnt.release(); touched.release();
     Cl.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
-    d_base.release(); filt.release();
+    d_base.release(); filt.release(); wave_end_of.release(); tab_theta.release();
     release_pool();
   };
   struct Guard {
@@ -785,6 +801,8 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(tab_off.alloc(Wmax, st));
   HSDL_TRY(tab_cap.alloc(Wmax, st));
   HSDL_TRY(filt.alloc((int64_t)Wmax * kSlotFilterWords, st));
+  HSDL_TRY(wave_end_of.alloc(n, st));
+  HSDL_TRY(tab_theta.alloc(Wmax, st));
   int64_t tab_cap_entries = 1 << 16;
   HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
   HSDL_TRY(ctr.alloc(1, st));
@@ -840,7 +858,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_CUDA(cudaGetLastError());
 #define HSDL_PRUNE(G, P, GRID)                                                                              \
   k_prune<G, P><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,             \
-                                           tab_cap.p, tab.p, stride, filt.p, Fout, wl_v.p, wl_key.p, wl_par.p, \
+                                           tab_cap.p, tab.p, stride, filt.p, tab_theta.p, Fout, wl_v.p, wl_key.p, wl_par.p, \
                                            ctr.p)
       if (pairs == 2) {
         if (lanes == 8) HSDL_PRUNE(8, 2, g_prune8);
@@ -882,7 +900,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     }
     for (int attempt = 0;; attempt++) {
       HSDL_CUDA(cudaMemsetAsync(ctr.p, 0, sizeof(Counters), st));
-      k_wave_init<<<(W + 255) / 256, 256, 0, st>>>(W, s_hub, map, cand.p, Cl.p, Fa.p, ctr.p);
+      k_wave_init<<<(W + 255) / 256, 256, 0, st>>>(W, s_hub, map, cand.p, Cl.p, Fa.p, ctr.p, wave_end_of.p);
       HSDL_LAUNCHED();
       k_table_size<<<1, 1024, 0, st>>>(W, s_hub, row_len.p, tab_cap.p, tab_off.p, ctr.p);
       HSDL_LAUNCHED();
@@ -897,7 +915,8 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
         HSDL_CUDA(cudaMemsetAsync(tab.p, 0x7F, (size_t)tab_need * stride * sizeof(int32_t), st));
         HSDL_CUDA(cudaMemsetAsync(filt.p, 0, (size_t)W * kSlotFilterWords * sizeof(uint32_t), st));
         k_table_fill<<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(W, s_hub, rows, row_len.p, tab_off.p,
-                                                                   tab_cap.p, tab.p, stride, filt.p);
+                                                                   tab_cap.p, tab.p, stride, filt.p, wave_end_of.p,
+                                                                   tab_theta.p);
         HSDL_LAUNCHED();
         k_table_prefix<<<grid, 256, 0, st>>>(ctr.p, tab.p, stride, K);
         HSDL_LAUNCHED();
@@ -991,7 +1010,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   }
   // only the rows and the pool are needed from here on
   cand.release(); cnt.release(); touched.release(); Cl.release(); Fa.release(); Fb.release(); wl_v.release();
-  wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); filt.release();
+  wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); filt.release(); wave_end_of.release(); tab_theta.release();
 
   // --- finalize: exact CSR with self labels, rows sorted by key ------------
   DevBuf<int64_t> flen;
