@@ -102,6 +102,8 @@ SIGNATURES = {
     "hsdl_validate_csr": (C.c_int, [I32, P, P, P]),
     "hsdl_graph_create": (C.c_int, [I32, P, P, P, PP]),
     "hsdl_graph_destroy": (C.c_int, [P]),
+    "hsdl_graph_create_from_edges": (C.c_int, [I32, I64, P, P, P, I32, P, PP]),
+    "hsdl_graph_get_csr": (C.c_int, [P, C.POINTER(I32), C.POINTER(I64), P, P, P]),
     "hsdl_group_lp": (C.c_int, [P, I32, I32, P, C.POINTER(I32), C.POINTER(I32)]),
     "hsdl_build_opts_default": (None, [C.POINTER(hsdl_build_opts)]),
     "hsdl_wave_bounds": (C.c_int, [I32, C.POINTER(hsdl_build_opts), P, I32, C.POINTER(I32)]),

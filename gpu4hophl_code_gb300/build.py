@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhsdl.so")
 
-CUDA_SOURCES = ["api.cu", "gen.cu", "clean.cu", "query.cu", "query_static.cu", "serve.cu", "lp.cu", "batched.cu", "prims.cu", "tune.cu"]
+CUDA_SOURCES = ["api.cu", "gen.cu", "clean.cu", "query.cu", "query_static.cu", "serve.cu", "lp.cu", "batched.cu", "prims.cu", "tune.cu", "graph_dev.cu"]
 CXX_SOURCES = ["graph_gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -341,6 +341,38 @@ int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, con
   return HSDL_OK;
 }
 
+int hsdl_graph_create_from_edges(int32_t n, int64_t m, const int32_t* a, const int32_t* b, const int32_t* w,
+                                 int32_t rank_by_degree, int32_t* new_to_old, hsdl_graph** out) {
+  HSDL_CHECK_ARG(out, "null output");
+  HSDL_CHECK_ARG(n >= 1 && n <= (int32_t)kIdMask, "vertex count out of range");
+  HSDL_CHECK_ARG(m >= 0 && (m == 0 || (a && b && w)), "bad edge arrays");
+  auto* g = new hsdl_graph();
+  const int rc = build_graph_from_edges(n, m, a, b, w, rank_by_degree != 0, new_to_old, g);
+  if (rc != HSDL_OK) {
+    delete g;
+    return rc;
+  }
+  *out = g;
+  return HSDL_OK;
+}
+
+int hsdl_graph_get_csr(hsdl_graph* g, int32_t* n, int64_t* adj_entries, int64_t* row_ptr, int32_t* col, int32_t* w) {
+  HSDL_CHECK_ARG(g, "null graph");
+  if (n) *n = g->n;
+  if (adj_entries) *adj_entries = g->m2;
+  HSDL_CUDA(cudaDeviceSynchronize());
+  if (row_ptr) std::copy(g->h_rp.begin(), g->h_rp.end(), row_ptr);
+  if ((col || w) && g->m2 > 0) {
+    std::vector<int2> adj((size_t)g->m2);
+    HSDL_CUDA(cudaMemcpy(adj.data(), g->adj.p, sizeof(int2) * g->m2, cudaMemcpyDeviceToHost));
+    for (int64_t e = 0; e < g->m2; e++) {
+      if (col) col[e] = adj[e].x;
+      if (w) w[e] = adj[e].y;
+    }
+  }
+  return HSDL_OK;
+}
+
 int hsdl_graph_destroy(hsdl_graph* g) {
   if (!g) return HSDL_OK;
   g->rp.release();

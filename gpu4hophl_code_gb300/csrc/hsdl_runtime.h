@@ -153,6 +153,9 @@ struct BatchPlan {
 int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl_index_impl* idx,
                 const BatchPlan* plan = nullptr, int32_t hub_limit = 0);
 int clean_index(hsdl_index_impl* idx);
+// Device degree ranking + CSR from a host edge list (graph_dev.cu).
+int build_graph_from_edges(int32_t n, int64_t m, const int32_t* a, const int32_t* b, const int32_t* w,
+                           bool rank_by_degree, int32_t* h_new_to_old, hsdl_graph_impl* g);
 int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,
              int32_t* iterations_run);
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,

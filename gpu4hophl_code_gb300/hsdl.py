@@ -125,11 +125,41 @@ class HostGraph:
 class Graph:
     """CSR graph resident in HBM."""
 
-    def __init__(self, g: HostGraph):
+    def __init__(self, g: "HostGraph | None"):
+        self._h = C.c_void_p()
+        self.new_to_old = None
+        if g is None:  # filled by from_edges
+            self.n, self.host = 0, None
+            return
         self.n = g.n
         self.host = g
-        self._h = C.c_void_p()
         check(lib().hsdl_graph_create(g.n, _ptr(g.row_ptr), _ptr(g.col), _ptr(g.w), C.byref(self._h)))
+
+    @classmethod
+    def from_edges(cls, n: int, a, b, w, rank_by_degree: bool = True) -> "Graph":
+        """Device graph from an undirected simple edge list, ranked and laid out
+        as CSR on the GPU (hsdl_graph_create_from_edges); `new_to_old` holds
+        each ranked vertex's original id."""
+        a = np.ascontiguousarray(a, np.int32)
+        b = np.ascontiguousarray(b, np.int32)
+        w = np.ascontiguousarray(w, np.int32)
+        g = cls(None)
+        g.n = n
+        g.new_to_old = np.zeros(n, np.int32)
+        check(lib().hsdl_graph_create_from_edges(n, len(a), _ptr(a), _ptr(b), _ptr(w), int(rank_by_degree),
+                                                 _ptr(g.new_to_old), C.byref(g._h)))
+        return g
+
+    def csr(self):
+        """(row_ptr int64[n+1], col int32[2m], w int32[2m]) copied from the device."""
+        n = C.c_int32()
+        adj = C.c_int64()
+        check(lib().hsdl_graph_get_csr(self._h, C.byref(n), C.byref(adj), None, None, None))
+        rp = np.zeros(n.value + 1, np.int64)
+        col = np.zeros(max(1, adj.value), np.int32)
+        w = np.zeros(max(1, adj.value), np.int32)
+        check(lib().hsdl_graph_get_csr(self._h, None, None, _ptr(rp), _ptr(col), _ptr(w)))
+        return rp, col[: adj.value], w[: adj.value]
 
     @property
     def handle(self):

@@ -89,6 +89,21 @@ typedef struct hsdl_graph hsdl_graph;
 int hsdl_graph_create(int32_t n, const int64_t* row_ptr, const int32_t* col, const int32_t* w,
                       hsdl_graph** out);
 int hsdl_graph_destroy(hsdl_graph* g);
+/* Builds the device graph from an undirected simple edge list (a[i], b[i],
+ * w[i], host arrays) on the GPU: degree ranking, largest degree first and ties
+ * by smaller id, then the CSR with rows sorted by neighbour - bit-identical to
+ * hsdl_host_graph_from_edges followed by hsdl_graph_create, without the host
+ * work.  Replaces graph_v_of_v_update_vertexIDs_by_degrees_large_to_small
+ * (CPU_HopHL/include/graph_v_of_v/graph_v_of_v_update_vertexIDs_by_degrees_large_to_small.h:14-40)
+ * and toCSR (Hybrid_Generation_Clean/include/graph/csr_graph.hpp:38-115) run
+ * on the host.  rank_by_degree = 0 keeps the ids.  new_to_old (n entries, may
+ * be NULL) receives the original id of each ranked vertex. */
+int hsdl_graph_create_from_edges(int32_t n, int64_t m, const int32_t* a, const int32_t* b, const int32_t* w,
+                                 int32_t rank_by_degree, int32_t* new_to_old, hsdl_graph** out);
+/* Copies a device graph's CSR to host arrays: row_ptr[n+1], col[adj], w[adj]
+ * (any of the three may be NULL to skip it); *n and *adj_entries receive the
+ * sizes. */
+int hsdl_graph_get_csr(hsdl_graph* g, int32_t* n, int64_t* adj_entries, int64_t* row_ptr, int32_t* col, int32_t* w);
 
 /* ------------------------------------------------------------------------
  * Label-propagation grouping.  Replaces generate_Group_CDLP(graph, groups,
