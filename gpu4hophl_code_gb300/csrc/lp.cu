@@ -23,7 +23,6 @@
 // The host merge and ordering then follow the reference's rules exactly.
 #include <algorithm>
 #include <chrono>
-#include <set>
 #include <vector>
 
 #include "hsdl_device.cuh"
@@ -210,63 +209,114 @@ __global__ void k_lp_apply(int32_t n, const int32_t* __restrict__ label, const i
 
 // Host side of generate_Group_CDLP (CDLP_group.cuh:39-100): bucket by label,
 // merge small groups greedily, order by total degree.
-struct GroupUnit {
-  int64_t id, size;
-  std::vector<int32_t> nodes;
-  bool operator<(const GroupUnit& b) const { return size == b.size ? id < b.id : size < b.size; }
-};
-
+// The reference's rules with flat arrays: labels bucketed by a counting sort
+// (each bucket's vertices ascending), groups kept in per-size stacks with a
+// bitmap of non-empty sizes, merged groups as chains of buckets.  A set of
+// node-vector groups did the same in 0.35 s at n = 1M (most of the grouping's
+// time); this takes milliseconds.
 void assemble_groups(int32_t n, const int32_t* label, const int64_t* rp, int32_t gmax,
                      std::vector<std::vector<int32_t>>& groups) {
-  std::vector<std::vector<int32_t>> buckets((size_t)n);
-  for (int32_t v = 0; v < n; v++) buckets[label[v]].push_back(v);
-  std::vector<std::vector<int32_t>> nonempty;
-  for (auto& b : buckets)
-    if (!b.empty()) nonempty.push_back(std::move(b));
-  std::set<GroupUnit> se;
-  for (size_t g = 0; g < nonempty.size(); g++) se.insert(GroupUnit{(int64_t)g, (int64_t)nonempty[g].size(), nonempty[g]});
-  std::vector<std::vector<int32_t>> after;
-  // take the largest group; merge it with the largest other group that still
-  // fits (CDLP_group.cuh:56-82)
-  while (!se.empty()) {
-    auto it1 = std::prev(se.end());
-    int64_t room = gmax - it1->size;
-    auto it2 = se.upper_bound(GroupUnit{(int64_t)nonempty.size(), room, {}});
-    bool merged = false;
-    if (it2 != se.begin()) {
-      --it2;
-      if (it2 == it1) {
-        if (it2 != se.begin()) {
-          --it2;
-        } else {
-          it2 = se.end();
-        }
-      }
-      if (it2 != se.end() && it2 != it1 && it1->size + it2->size <= gmax) {
-        GroupUnit a = *it1, b = *it2;
-        a.size += b.size;
-        a.nodes.insert(a.nodes.end(), b.nodes.begin(), b.nodes.end());
-        se.erase(it1);
-        se.erase(it2);
-        se.insert(a);
-        merged = true;
-      }
+  // buckets of vertices by label, in label order
+  std::vector<int64_t> start((size_t)n + 1, 0);
+  for (int32_t v = 0; v < n; v++) start[(size_t)label[v] + 1]++;
+  for (int32_t c = 0; c < n; c++) start[(size_t)c + 1] += start[c];
+  std::vector<int32_t> members((size_t)n);
+  {
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int32_t v = 0; v < n; v++) members[(size_t)fill[label[v]]++] = v;
+  }
+  std::vector<int32_t> part_label;  // group g = the g-th non-empty bucket
+  for (int32_t c = 0; c < n; c++)
+    if (start[(size_t)c + 1] > start[c]) part_label.push_back(c);
+  const int64_t G = (int64_t)part_label.size();
+  std::vector<int64_t> size((size_t)G), tail((size_t)G), next((size_t)G, -1);
+  // groups ordered by (size, id): per-size max-heaps of ids; sizes above gmax
+  // (only unmerged buckets can be that large) share the last stack, ordered
+  // by (size, id) themselves
+  const int64_t S = (int64_t)gmax + 1;
+  std::vector<std::vector<int64_t>> by_size((size_t)S + 1);
+  std::vector<uint64_t> nonempty((size_t)(S + 64) / 64 + 1, 0);
+  std::vector<std::pair<int64_t, int64_t>> big;  // (size, id) of groups larger than gmax, kept sorted
+  auto push = [&](int64_t g) {
+    if (size[g] > gmax) {
+      big.insert(std::upper_bound(big.begin(), big.end(), std::make_pair(size[g], g)), std::make_pair(size[g], g));
+      return;
     }
-    if (!merged) {
-      after.push_back(it1->nodes);
-      se.erase(it1);
+    auto& h = by_size[(size_t)size[g]];
+    h.push_back(g);
+    std::push_heap(h.begin(), h.end());
+    nonempty[(size_t)size[g] / 64] |= 1ull << (size[g] % 64);
+  };
+  auto pop = [&](int64_t s) {
+    auto& h = by_size[(size_t)s];
+    std::pop_heap(h.begin(), h.end());
+    const int64_t g = h.back();
+    h.pop_back();
+    if (h.empty()) nonempty[(size_t)s / 64] &= ~(1ull << (s % 64));
+    return g;
+  };
+  // largest non-empty size <= lim (0 if none)
+  auto highest = [&](int64_t lim) -> int64_t {
+    if (lim <= 0) return 0;
+    lim = std::min(lim, (int64_t)gmax);
+    for (int64_t w = lim / 64; w >= 0; w--) {
+      uint64_t bits = nonempty[(size_t)w];
+      if (w == lim / 64) bits &= (lim % 64 == 63) ? ~0ull : ((1ull << (lim % 64 + 1)) - 1);
+      if (bits) return w * 64 + (63 - __builtin_clzll(bits));
+    }
+    return 0;
+  };
+  for (int64_t g = 0; g < G; g++) {
+    size[g] = start[(size_t)part_label[g] + 1] - start[part_label[g]];
+    tail[g] = g;
+    push(g);
+  }
+  std::vector<int64_t> after;  // finished groups (their head bucket), in order
+  int64_t live = G;
+  while (live > 0) {
+    // the largest group (size, then id)
+    int64_t g1;
+    if (!big.empty()) {
+      g1 = big.back().second;
+      big.pop_back();
+    } else {
+      g1 = pop(highest(gmax));
+    }
+    live--;
+    // the largest other group that still fits (CDLP_group.cuh:56-82)
+    const int64_t s2 = highest(gmax - size[g1]);
+    if (s2 > 0) {
+      const int64_t g2 = pop(s2);
+      next[tail[g1]] = g2;
+      tail[g1] = tail[g2];
+      size[g1] += size[g2];
+      push(g1);
+    } else {
+      after.push_back(g1);
     }
   }
   // order by total degree, largest first (ties by position)
-  std::vector<GroupUnit> order;
-  for (size_t g = 0; g < after.size(); g++) {
+  std::vector<std::pair<int64_t, int64_t>> order;  // (-total degree, position)
+  order.reserve(after.size());
+  for (size_t i = 0; i < after.size(); i++) {
     int64_t tot = 0;
-    for (int32_t v : after[g]) tot -= rp[v + 1] - rp[v];
-    order.push_back(GroupUnit{(int64_t)g, tot, after[g]});
+    for (int64_t p = after[i]; p >= 0; p = next[p])
+      for (int64_t j = start[part_label[p]]; j < start[(size_t)part_label[p] + 1]; j++) {
+        const int32_t v = members[(size_t)j];
+        tot -= rp[v + 1] - rp[v];
+      }
+    order.push_back({tot, (int64_t)i});
   }
   std::sort(order.begin(), order.end());
   groups.clear();
-  for (auto& u : order) groups.push_back(std::move(u.nodes));
+  groups.reserve(order.size());
+  for (auto& o : order) {
+    std::vector<int32_t> nodes;
+    for (int64_t p = after[(size_t)o.second]; p >= 0; p = next[p])
+      nodes.insert(nodes.end(), members.begin() + start[part_label[p]],
+                   members.begin() + start[(size_t)part_label[p] + 1]);
+    groups.push_back(std::move(nodes));
+  }
 }
 
 int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_of_vertex, int32_t* num_groups,

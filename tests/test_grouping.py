@@ -40,7 +40,7 @@ def test_oracle_greedy_merge_leaves_no_mergeable_pair(orc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gmax,iters", [(1024, 100), (64, 20), (5, 10)])
+@pytest.mark.parametrize("gmax,iters", [(1024, 100), (64, 20), (5, 10), (1024, 1), (3000, 2)])
 def test_gpu_grouping_matches_oracle(orc, gmax, iters):
     for g in _graphs():
         dev = H.Graph(g)
