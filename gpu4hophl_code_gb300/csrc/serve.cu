@@ -443,7 +443,23 @@ int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
   auto* S = new hsdl_server();
   S->opts = o;
   S->sms = device_sm_count();
-  if (S->opts.ctas <= 0) S->opts.ctas = S->sms * 2;
+  {
+    // every block of the persistent loop must be resident at once (a block
+    // left waiting for a slot would hold its share of the tickets)
+    const int per_sm = o.lanes_per_query == 8    ? resident_blocks(k_serve<8>, 256)
+                       : o.lanes_per_query == 16 ? resident_blocks(k_serve<16>, 256)
+                                                 : resident_blocks(k_serve<32>, 256);
+    const int most = S->sms * per_sm;
+    // default 4 per SM: at n = 1M, 2 / 3 / 4 / 5 blocks of 256 threads per SM
+    // saturated at 147 / 205 / 241 / 253 M q/s, and 4 still held p99 under
+    // 1 ms at 200 M q/s offered (5 raised latency at every load)
+    if (S->opts.ctas <= 0) S->opts.ctas = std::min(most, S->sms * 4);
+    if (S->opts.ctas > most) {
+      delete S;
+      set_error("ctas must be at most " + std::to_string(most) + " (blocks of the loop that fit on the GPU at once)");
+      return HSDL_ERR_INVALID;
+    }
+  }
   S->cap = 1ull << o.ring_log2;
   S->mask = S->cap - 1;
   auto fail = [&](int rc) {
