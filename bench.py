@@ -120,14 +120,16 @@ def make_queries(n, nq, K, seed):
     return s, t, k
 
 
-def algorithmic_bytes(off: np.ndarray, s, t, k) -> int:
-    """Per query: the label keys of both rows (8 B each: hub:32 | hop:4 |
-    distance:28; the join must read every one), the four row offsets (32 B),
-    the (s,t,k) record in (12 B) and the answer out (4 B)."""
+def algorithmic_bytes(off: np.ndarray, s, t, k, per_label: int = 12) -> int:
+    """Per query: per_label bytes for every label of both rows (the join must
+    read every one) and 32 B for the two offset pairs - the per-query figure
+    12 (|L_s| + |L_t|) + 32 of the hot-path scope, which counts a label as its
+    (hub, hop, distance) triple.  The index stores 8 bytes per label (hub:32 |
+    hop:4 | distance:28); per_label = 8 gives that count."""
     ln = np.diff(off)
     rows = ln[s].astype(np.int64) + ln[t].astype(np.int64)
     rows[s == t] = 0
-    return int(8 * rows.sum() + 48 * len(s))
+    return int(per_label * rows.sum() + 32 * len(s))
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_query_traffic_chung_lu_1m_10Mq.md")
@@ -322,12 +324,17 @@ def run_ours(args, dist, rank, world, local):
     if rank == 0:
         off, lab = idx.export()
         bytes_per_launch = algorithmic_bytes(off, s, t, k)
-        achieved = bytes_per_launch / (kernel_ms / 1000.0 / args.steps) / 1e9
+        launch_s = kernel_ms / 1000.0 / args.steps
+        achieved = bytes_per_launch / launch_s / 1e9
+        packed = algorithmic_bytes(off, s, t, k, per_label=8)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": captured_traffic(args),
                 "kernel": "k_query", "algorithmic_bytes_per_launch": bytes_per_launch,
-                "bytes_per_query": round(bytes_per_launch / args.queries, 1)}
+                "bytes_per_query": round(bytes_per_launch / args.queries, 1),
+                "byte_model": "12 B per label of both rows + 32 B of row offsets per query",
+                "stored_key_bytes": {"per_launch": packed, "achieved": round(packed / launch_s / 1e9, 1),
+                                     "frac": round(packed / launch_s / 1e9 / peak, 4)}}
         cpu = None
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
