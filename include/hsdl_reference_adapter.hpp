@@ -25,6 +25,7 @@
 // hsdl_gpu::error carrying hsdl_last_error().
 #pragma once
 
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <stdexcept>
