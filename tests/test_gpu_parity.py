@@ -256,3 +256,28 @@ def test_query_batch_rejects_vertices_outside_the_index():
             idx.query(s2, t2, k)
         assert f"at query {at}" in str(e.value)
     assert np.array_equal(idx.query(s, t, k), ok)  # the index is unaffected
+
+
+@pytest.mark.parametrize("K,wmax", [(14, 19_000_000), (1, 250_000_000), (3, 80_000_000)])
+def test_hop_bound_and_weight_limits(orc, K, wmax):
+    """The largest hop bound (14) and weights near the 28-bit distance limit
+    (K * max weight < 2^28): labels and answers still equal the oracle's."""
+    g = H.HostGraph.erdos_renyi(400, 1600, max(1, wmax // 2), wmax, seed=K + 40)
+    dev, idx = gpu_build(g, K)
+    off, lab = idx.export()
+    ref = orc.build(g, K, threads=1)
+    assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
+    rng = np.random.default_rng(K)
+    s = rng.integers(0, g.n, 20000).astype(np.int32)
+    t = rng.integers(0, g.n, 20000).astype(np.int32)
+    k = rng.integers(0, K + 2, 20000).astype(np.int32)
+    got = idx.query(s, t, k)
+    assert np.array_equal(got, orc.query(ref, s, t, k))
+    assert got[(got != 2147483647)].max() < (1 << 28)
+
+
+def test_build_rejects_weights_past_the_distance_limit():
+    g = H.HostGraph.erdos_renyi(100, 300, 100_000_000, 100_000_000, seed=3)
+    dev = H.Graph(g)
+    with pytest.raises(H.HsdlError):
+        H.Index.build(dev, 3)  # 3 * 1e8 >= 2^28
