@@ -273,7 +273,8 @@ def test_hop_bound_and_weight_limits(orc, K, wmax):
     k = rng.integers(0, K + 2, 20000).astype(np.int32)
     got = idx.query(s, t, k)
     assert np.array_equal(got, orc.query(ref, s, t, k))
-    assert got[(got != 2147483647)].max() < (1 << 28)
+    assert lab[:, 3].max() < (1 << 28)  # each label's distance fits its 28-bit field
+    assert got[(got != 2147483647)].max() >= wmax // 2  # the answers do carry the large weights
 
 
 def test_build_rejects_weights_past_the_distance_limit():
