@@ -43,7 +43,7 @@ namespace hsdl {
 
 namespace {
 
-constexpr int kCleanThreads = 256;
+constexpr int kCleanThreads = 512;  // 256 / 512 / 1024 threads: clean 0.275 / 0.207 / 0.220 s at n = 1M
 // Membership filter of v's hubs: one bit per hash value of a hub id, 65,536
 // bits in shared memory.  Most hubs of L[u] are not hubs of v; a clear bit
 // answers those with one shared-memory load instead of a probe sequence
