@@ -184,15 +184,24 @@ int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int6
   int32_t* count = nullptr;
   HSDL_CUDA(cudaMallocAsync(&rows, (size_t)n * sizeof(int32_t), st));
   HSDL_CUDA(cudaMallocAsync(&count, sizeof(int32_t), st));
-  // shared-memory rows: up to 8192 labels (8192 * 12 B = 96 KB)
-  const int smem_cap = 8192;
+  // shared-memory rows: up to 1024 labels in 12 KB blocks of 256 threads (many
+  // per SM), up to 8192 labels (96 KB) in blocks of 512
+  const int small_cap = 1024, smem_cap = 8192;
   const size_t smem = (size_t)smem_cap * (sizeof(uint64_t) + sizeof(int32_t));
+  const size_t small_smem = (size_t)small_cap * (sizeof(uint64_t) + sizeof(int32_t));
   HSDL_CUDA(cudaFuncSetAttribute(k_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   HSDL_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
-  k_list_large_rows<<<sms * 4, 256, 0, st>>>(n, d_off, rows, count, 32, smem_cap);
+  k_list_large_rows<<<sms * 4, 256, 0, st>>>(n, d_off, rows, count, 32, small_cap);
   HSDL_LAUNCHED();
-  k_sort_large<<<sms * 2, 512, smem, st>>>(rows, count, d_off, key, par, smem_cap, nullptr, nullptr);
+  k_sort_large<<<sms * 8, 256, small_smem, st>>>(rows, count, d_off, key, par, small_cap, nullptr, nullptr);
   HSDL_LAUNCHED();
+  if (max_row > small_cap) {
+    HSDL_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
+    k_list_large_rows<<<sms * 4, 256, 0, st>>>(n, d_off, rows, count, small_cap, smem_cap);
+    HSDL_LAUNCHED();
+    k_sort_large<<<sms * 2, 512, smem, st>>>(rows, count, d_off, key, par, smem_cap, nullptr, nullptr);
+    HSDL_LAUNCHED();
+  }
   if (max_row > smem_cap) {
     int64_t P = 1;
     while (P < max_row) P <<= 1;
