@@ -135,7 +135,9 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
                          (uint32_t)x.distance <= kDistMask,
                      "label field out of range at entry " + std::to_string(i));
       uint64_t key = lkey((uint32_t)x.hub_vertex, (uint32_t)x.hop, (uint32_t)x.distance);
-      HSDL_CHECK_ARG(i == offsets[v] || prev < key,
+      // equal labels may repeat: the reference's 2023WWW generation pushes a
+      // label once per improving relaxation (generation.h:276-336)
+      HSDL_CHECK_ARG(i == offsets[v] || prev <= key,
                      "row " + std::to_string(v) + " is not sorted by (hub, hop, distance)");
       prev = key;
       keys[i] = key;
@@ -415,6 +417,7 @@ static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
   HSDL_CHECK_ARG(o->prune_lanes == 0 || o->prune_lanes == 8 || o->prune_lanes == 16 || o->prune_lanes == 32,
                  "prune_lanes must be 0, 8, 16 or 32");
   HSDL_CHECK_ARG(o->prune_pairs >= 0 && o->prune_pairs <= 2, "prune_pairs must be 0, 1 or 2");
+  HSDL_CHECK_ARG(o->generation == 0 || o->generation == 1, "generation must be 0 (HSDL) or 1 (2023WWW)");
   return HSDL_OK;
 }
 

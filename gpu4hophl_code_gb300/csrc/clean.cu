@@ -17,6 +17,13 @@
 // (u, 0, 0), so for hub w = u the check uses v's labels of hub u with fewer
 // than h hops.  Every label is therefore decided independently.
 //
+// Only hubs ranked above u are witnesses: in the reference's walk over the
+// sorted L[v], the accepted labels of v when (u, h, d) comes up have hubs
+// ranked at or above u.  For labels of the HSDL search every hub of L[u] is
+// ranked at or above u anyway; labels of the 2023WWW search (no rank prune)
+// also put hubs ranked below u into L[u], and those are skipped.  below[u]
+// counts the labels of the sorted L[u] with hubs ranked above u (its prefix).
+//
 // Wave window.  For labels generated by the wave engine, the pruning query of
 // u's search already saw every pair through a hub w of an earlier wave: both
 // w's label of u and w's label of v were committed before u's wave, and the
@@ -24,8 +31,8 @@
 // (ranked above u), whose labels were committed with u's.  So when the index
 // records each hub's wave (wave_lo[u] = the wave's first hub), a label (u, h, d)
 // of v is checked against the hubs w of L[u] with wave_lo[u] <= w < u - the
-// tail of the sorted row - plus u's own fewer-hop labels of v.  Without the
-// record (an imported label set) the whole of L[u] is scanned.
+// tail of the prefix below[u] - plus u's own fewer-hop labels of v.  Without
+// the record (an imported label set) the whole prefix is scanned.
 //
 // Kernel: one block per vertex v (persistent blocks take vertices from a work
 // counter).  The block builds v's hop-prefix-min table T_v (hash on hub id, in
@@ -69,6 +76,7 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
                                                          const uint64_t* __restrict__ key,
                                                          uint8_t* __restrict__ keep, int64_t* __restrict__ kept,
                                                          const int32_t* __restrict__ wave_lo,
+                                                         const int32_t* __restrict__ below,
                                                          int smem_slots, int32_t* __restrict__ gscratch,
                                                          int64_t gscratch_slots, int* __restrict__ next_v,
                                                          unsigned long long* __restrict__ reads) {
@@ -136,19 +144,26 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
       bool keepit;
       if (u == v) {
         keepit = true;  // the self label (v, 0, 0) is never covered
+      } else if (i > 0 && (key[lo + i - 1] >> 28) == (kv >> 28)) {
+        // the row's previous label has the same hub and hop and a distance
+        // <= d: once accepted it covers this one through u's self label, as
+        // in the reference; if it was covered, so is this one.  (Only
+        // imported label sets repeat a (hub, hop); a generated row has one
+        // label per hub and hop.)
+        keepit = false;
       } else {
         long long q = LLONG_MAX;
         // hub u itself: labels of v with hub u and fewer hops
         const int su = tab_find(Tk, mask, u);
         if (su >= 0 && Td[(int64_t)su * R + h - 1] != kInf32) q = Td[(int64_t)su * R + h - 1];
         if (!(q <= d)) {
-          // L[u] is sorted by hub and its hubs are ranked at or above u, so
-          // the hubs of u's own wave are its tail: scan 32 labels at a time
-          // from the end while the chunk's first hub is still in the window.
+          // L[u] is sorted by hub, so the hubs ranked above u are its prefix
+          // [0, below[u]) and the hubs of u's own wave the prefix's tail:
+          // scan 32 labels at a time from the prefix's end while the chunk's
+          // first hub is still in the window.
           const int64_t ulo = off[u];
-          const int ulen = (int)(off[u + 1] - ulo);
           const int ws = wave_lo ? wave_lo[u] : 0;
-          for (int j1 = ulen; j1 > 0; j1 -= 32) {
+          for (int j1 = below[u]; j1 > 0; j1 -= 32) {
             const int j = j1 - 32 + lane;
             bool in_window = false;
             if (j >= 0) {
@@ -188,6 +203,22 @@ __global__ void __launch_bounds__(kCleanThreads) k_clean(int32_t n, int32_t K, c
       kept[v] = s;
     }
     __syncthreads();
+  }
+}
+
+// below[u] = labels of the sorted row L[u] whose hub is ranked above u (the
+// first index with hub >= u, by binary search over the keys).
+__global__ void k_below(int32_t n, const int64_t* __restrict__ off, const uint64_t* __restrict__ key,
+                        int32_t* __restrict__ below) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const uint64_t first = (uint64_t)(uint32_t)u << 32;
+    int64_t a = off[u], b = off[u + 1];
+    const int64_t lo = a;
+    while (a < b) {
+      const int64_t mid = (a + b) >> 1;
+      if (key[mid] < first) a = mid + 1; else b = mid;
+    }
+    below[u] = (int32_t)(a - lo);
   }
 }
 
@@ -249,8 +280,12 @@ int clean_index(hsdl_index_impl* idx) {
   HSDL_TRY(noff.alloc((int64_t)n + 1, st));
   HSDL_TRY(next.alloc(1, st));
   HSDL_CUDA(cudaMemsetAsync(next.p, 0, sizeof(int), st));
-  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->key.p, keep.p, kept.p,
-                                             idx->wave_lo.p, smem_slots, gscratch.p, gslots, next.p, reads.p);
+  DevBuf<int32_t> below;
+  HSDL_TRY(below.alloc(std::max<int32_t>(1, n), st));
+  k_below<<<sms * 8, 256, 0, st>>>(n, idx->off.p, idx->key.p, below.p);
+  HSDL_LAUNCHED();
+  k_clean<<<grid, kCleanThreads, smem, st>>>(n, K, idx->off.p, idx->key.p, keep.p, kept.p, idx->wave_lo.p,
+                                             below.p, smem_slots, gscratch.p, gslots, next.p, reads.p);
   HSDL_LAUNCHED();
   HSDL_TRY(exclusive_scan_i64(kept.p, noff.p, n, st));
   int64_t total = 0;
@@ -279,6 +314,7 @@ int clean_index(hsdl_index_impl* idx) {
   gscratch.release();
   next.release();
   reads.release();
+  below.release();
   idx->wave_lo.release();  // the clean is done; a repeat would need the full scan
   idx->work_clean_reads += (int64_t)h_reads;
   idx->before = idx->total;

@@ -258,13 +258,14 @@ __global__ void k_table_prefix(const Counters* ctr, int32_t* __restrict__ tab, i
 // ---------------------------------------------------------------------------
 // Each block takes `tiles` tiles of TPB frontier entries at a time from a
 // per-hop counter, so a block that drew heavy vertices takes fewer tiles.
-// Only neighbours ranked below the hub are relaxed (rank prune,
-// generation.h:107-110); rows are sorted by neighbour id, so they are the
-// suffix after the hub's id, found by binary search.  The tile's relaxations
-// are spread evenly over the block through an exclusive scan of the suffix
-// lengths.
+// With rank_prune (the HSDL search) only neighbours ranked below the hub are
+// relaxed (generation.h:107-110); rows are sorted by neighbour id, so they
+// are the suffix after the hub's id, found by binary search.  Without it (the
+// 2023WWW search, generation.h:338-347) every neighbour is relaxed.  The
+// tile's relaxations are spread evenly over the block through an exclusive
+// scan of the row lengths.
 template <int TPB>
-__global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t K, int32_t tiles,
+__global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t K, int32_t rank_prune, int32_t tiles,
                                                 const int64_t* __restrict__ rp, const int2* __restrict__ adj,
                                                 const int4* __restrict__ F, uint64_t* __restrict__ cand,
                                                 int2* __restrict__ C, int64_t capC, Counters* ctr) {
@@ -289,13 +290,15 @@ __global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t 
         int hub = s_hub + e.x;
         lo = rp[e.y];
         int64_t hi = rp[e.y + 1];
-        int64_t a = lo, b = hi;
-        while (a < b) {
-          int64_t mid = (a + b) >> 1;
-          if (adj[mid].x <= hub) a = mid + 1; else b = mid;
+        if (rank_prune) {
+          int64_t a = lo, b = hi;
+          while (a < b) {
+            int64_t mid = (a + b) >> 1;
+            if (adj[mid].x <= hub) a = mid + 1; else b = mid;
+          }
+          lo = a;
         }
-        lo = a;
-        len = hi - a;
+        len = hi - lo;
       }
       int64_t total;
       int64_t pre = block_exclusive_scan(len, s_scan, &total);
@@ -347,7 +350,7 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 // read G labels of v at a time and stop as soon as one dominates.  Warps take
 // 8 candidates per group at a time from a per-hop counter, so candidates with
 // long label lists do not hold back a statically assigned share.
-template <int G, int P>
+template <int G, int P, bool SELF = false>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
                                                     Rows rows, const int32_t* __restrict__ row_len,
@@ -436,6 +439,14 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
             ix = (ix + 1) & mask;
           }
         };
+        // A candidate from an earlier wave (only the 2023WWW search, which
+        // has no rank prune, reaches one) also has its self label (v, 0, 0):
+        // the reference pushes it when v's own search starts, and here it is
+        // added to the rows only when the index is finalised.
+        if (SELF && v < s_hub && gl == 0) {
+          const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)v);
+          probe(lkey((uint32_t)v, 0, 0), __ldg(Fl + (fb >> 5)));
+        }
         // a step covers 2 P G labels: lane gl takes the pairs at 2 gl + 2 G p
         uint64_t a[2 * P];
 #pragma unroll
@@ -650,6 +661,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   cudaStream_t st = idx->stream;
   const int sms = device_sm_count();
   const int stride = (K + 2 <= 8) ? 8 : 16;  // hub-table slot: key + K+1 distances, 32 or 64 B
+  const int32_t rank_prune = opts.generation == 0 ? 1 : 0;  // the HSDL search; 0 = the 2023WWW search
   double t0 = now_s();
 
   size_t free_b = 0, total_b = 0;
@@ -819,12 +831,15 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
                               : tpb == 512 ? resident_blocks(k_expand<512>, 512)
                                            : resident_blocks(k_expand<256>, 256));
   const int pairs = opts.prune_pairs == 2 ? 2 : 1;
-  const int g_prune8 = sms * (pairs == 2 ? resident_blocks(k_prune<8, 2>, kThreads)
-                                         : resident_blocks(k_prune<8, 1>, kThreads));
-  const int g_prune16 = sms * (pairs == 2 ? resident_blocks(k_prune<16, 2>, kThreads)
-                                          : resident_blocks(k_prune<16, 1>, kThreads));
-  const int g_prune32 = sms * (pairs == 2 ? resident_blocks(k_prune<32, 2>, kThreads)
-                                          : resident_blocks(k_prune<32, 1>, kThreads));
+  const int g_prune8 = sms * (!rank_prune ? resident_blocks(k_prune<8, 1, true>, kThreads)
+                              : pairs == 2 ? resident_blocks(k_prune<8, 2>, kThreads)
+                                           : resident_blocks(k_prune<8, 1>, kThreads));
+  const int g_prune16 = sms * (!rank_prune ? resident_blocks(k_prune<16, 1, true>, kThreads)
+                               : pairs == 2 ? resident_blocks(k_prune<16, 2>, kThreads)
+                                            : resident_blocks(k_prune<16, 1>, kThreads));
+  const int g_prune32 = sms * (!rank_prune ? resident_blocks(k_prune<32, 1, true>, kThreads)
+                               : pairs == 2 ? resident_blocks(k_prune<32, 2>, kThreads)
+                                            : resident_blocks(k_prune<32, 1>, kThreads));
   int lanes = 32;
 
   Counters hc;
@@ -848,26 +863,30 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       int4* Fin = (h & 1) ? Fa.p : Fb.p;
       int4* Fout = (h & 1) ? Fb.p : Fa.p;
       if (tpb == 128)
-        k_expand<128><<<g_expand, 128, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+        k_expand<128><<<g_expand, 128, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
       else if (tpb == 512)
-        k_expand<512><<<g_expand, 512, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+        k_expand<512><<<g_expand, 512, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
       else
-        k_expand<256><<<g_expand, 256, 0, st>>>(map, h, K, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+        k_expand<256><<<g_expand, 256, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
       HSDL_CUDA(cudaGetLastError());
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());
-#define HSDL_PRUNE(G, P, GRID)                                                                              \
-  k_prune<G, P><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,             \
-                                           tab_cap.p, tab.p, stride, filt.p, tab_theta.p, Fout, wl_v.p, wl_key.p, wl_par.p, \
-                                           ctr.p)
-      if (pairs == 2) {
-        if (lanes == 8) HSDL_PRUNE(8, 2, g_prune8);
-        else if (lanes == 16) HSDL_PRUNE(16, 2, g_prune16);
-        else HSDL_PRUNE(32, 2, g_prune32);
+#define HSDL_PRUNE(G, P, SELF, GRID)                                                                        \
+  k_prune<G, P, SELF><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,       \
+                                                 tab_cap.p, tab.p, stride, filt.p, tab_theta.p, Fout, wl_v.p, \
+                                                 wl_key.p, wl_par.p, ctr.p)
+      if (!rank_prune) {  // the 2023WWW search: candidates from earlier waves probe their self label
+        if (lanes == 8) HSDL_PRUNE(8, 1, true, g_prune8);
+        else if (lanes == 16) HSDL_PRUNE(16, 1, true, g_prune16);
+        else HSDL_PRUNE(32, 1, true, g_prune32);
+      } else if (pairs == 2) {
+        if (lanes == 8) HSDL_PRUNE(8, 2, false, g_prune8);
+        else if (lanes == 16) HSDL_PRUNE(16, 2, false, g_prune16);
+        else HSDL_PRUNE(32, 2, false, g_prune32);
       } else {
-        if (lanes == 8) HSDL_PRUNE(8, 1, g_prune8);
-        else if (lanes == 16) HSDL_PRUNE(16, 1, g_prune16);
-        else HSDL_PRUNE(32, 1, g_prune32);
+        if (lanes == 8) HSDL_PRUNE(8, 1, false, g_prune8);
+        else if (lanes == 16) HSDL_PRUNE(16, 1, false, g_prune16);
+        else HSDL_PRUNE(32, 1, false, g_prune32);
       }
 #undef HSDL_PRUNE
       HSDL_CUDA(cudaGetLastError());

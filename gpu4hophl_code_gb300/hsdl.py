@@ -199,8 +199,10 @@ def generate_Group_CDLP(instance_graph, groups: list, MAX_GROUP_SIZE: int, max_i
 
 
 def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block_threads: int = 0,
-               frontier_tile: int = 0, prune_lanes: int = 0, prune_pairs: int = 0,
+               frontier_tile: int = 0, prune_lanes: int = 0, prune_pairs: int = 0, generation: int = 0,
                device_budget_bytes: int = 0) -> N.hsdl_build_opts:
+    """generation: 0 = the HSDL search, 1 = the 2023WWW search (the
+    reference's use_2023WWW_generation); the cleaned labels are the same."""
     o = N.hsdl_build_opts()
     lib().hsdl_build_opts_default(C.byref(o))
     o.clean = int(clean)
@@ -210,6 +212,7 @@ def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block
     o.frontier_tile = frontier_tile
     o.prune_lanes = prune_lanes
     o.prune_pairs = prune_pairs
+    o.generation = generation
     o.device_budget_bytes = device_budget_bytes
     return o
 
@@ -437,14 +440,15 @@ def _as_host_graph(input_graph) -> HostGraph:
 def hop_constrained_two_hop_labels_generation(input_graph, case_info: hop_constrained_case_info) -> None:
     """hop_constrained_two_hop_labels_generation (generation.h:513-632): builds
     labels of a graph whose ids are ranks, fills case_info.L and the timers."""
-    if case_info.use_2023WWW_generation:
-        raise NotImplementedError("the 2023WWW generation variant is not part of this engine")
     if case_info.upper_k <= 0:
         raise ValueError("upper_k must be >= 1 (unbounded hops are not supported)")
     t0 = time.perf_counter()
     g = input_graph if isinstance(input_graph, Graph) else Graph(_as_host_graph(input_graph))
     t1 = time.perf_counter()
-    idx = Index.build(g, case_info.upper_k, clean=False, **case_info.build_options)
+    opts = dict(case_info.build_options)
+    if case_info.use_2023WWW_generation:
+        opts["generation"] = 1  # _2023WWW_thread_function (generation.h:226-370, selected at :568-574)
+    idx = Index.build(g, case_info.upper_k, clean=False, **opts)
     info = idx.info()
     case_info.time_initialization = t1 - t0
     case_info.time_generate_labels = info["time_generate_s"]

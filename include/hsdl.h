@@ -134,6 +134,11 @@ typedef struct hsdl_build_opts {
   int32_t frontier_tile;  /* frontier entries an expansion block takes at a time (0 = one block's worth) */
   int32_t prune_lanes;    /* lanes per candidate in the pruning join: 8, 16 or 32 (0 = per wave, by mean row length) */
   int32_t prune_pairs;    /* label pairs each lane of the pruning join loads per step: 1 or 2 (0 = 1) */
+  int32_t generation;     /* 0 = the HSDL search (HSDL_thread_function, generation.h:45-224; default);
+                             1 = the 2023WWW search (_2023WWW_thread_function, generation.h:226-370;
+                             the reference's use_2023WWW_generation): no rank prune, so more labels
+                             before the clean; the cleaned labels are the same */
+  int32_t reserved;       /* 0 */
   int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
 } hsdl_build_opts;
 
@@ -271,7 +276,9 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);
  * (hub, hop, distance), the reference's sortL order
  * (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:373-419). */
 int hsdl_export(hsdl_index* idx, int64_t* offsets, hsdl_label* labels);
-/* Builds an index from host labels (each row sorted as above). */
+/* Builds an index from host labels (each row sorted as above; equal labels
+ * may repeat, as in the reference's 2023WWW output before its clean, and the
+ * clean drops the repeats). */
 int hsdl_import(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label* labels, hsdl_index** out);
 /* Binary label file of Clean_pc/main.cu:11-58 (save_labels / load_labels):
  * size_t V; per vertex size_t count, then count x {hub, parent, hop, dist}. */

@@ -11,7 +11,7 @@
 //   Graph    - size() and operator[](v) yielding pairs (neighbour, weight),
 //              like graph_v_of_v<int> (CPU_HopHL/include/graph_v_of_v/
 //              graph_v_of_v.h:46-87); vertex ids must already be ranks.
-//   CaseInfo - fields upper_k, use_canonical_repair, time_initialization,
+//   CaseInfo - fields upper_k, use_2023WWW_generation, use_canonical_repair, time_initialization,
 //              time_generate_labels, time_sortL, time_canonical_repair,
 //              time_total, label_size_before_canonical_repair,
 //              label_size_after_canonical_repair,
@@ -119,6 +119,7 @@ void hop_constrained_two_hop_labels_generation(Graph& input_graph, CaseInfo& cas
   hsdl_build_opts o;
   hsdl_build_opts_default(&o);
   o.clean = 0;
+  o.generation = case_info.use_2023WWW_generation ? 1 : 0;  // generation.h:568-574
   hsdl_index* idx = nullptr;
   check(hsdl_build(g.get(), case_info.upper_k, &o, &idx));
   hsdl_index_info before;

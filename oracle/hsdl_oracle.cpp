@@ -7,7 +7,8 @@
 //
 // What it restates (reference file:line, paths inside the reference project):
 //   orc_build (generation)  CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:45-224
-//                           (HSDL_thread_function) and :513-632 (driver)
+//                           (HSDL_thread_function) and :513-632 (driver); variant 1:
+//                           same file :226-370 (_2023WWW_thread_function)
 //   sortL                   same file :373-419
 //   clean                   same file :422-511 (hop_constrained_clean_L)
 //   orc_query               CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:144-222
@@ -245,6 +246,87 @@ void hub_search(const Graph& g, int K, int hub, Scratch& S, const std::vector<La
   }
 }
 
+// Per-worker scratch of the 2023WWW search.
+struct WwwScratch {
+  std::vector<int32_t> dist, pred;                               // dist_hop: best distance so far, its predecessor
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> hubtab;  // Temp_L_vk: (dist, hop) of L[hub] per hub
+  std::vector<int32_t> touched, touched_hubs;
+  WwwScratch(int n) : dist(n, INT_MAX), pred(n, 0), hubtab(n) {}
+};
+
+// One hub's 2023WWW search (_2023WWW_thread_function, generation.h:226-370):
+// hop-synchronous, no rank prune.  Vh[h] lists the vertices whose best
+// distance improved in hop h - 1 (once per improving relaxation, so a vertex
+// can appear, and be labelled, more than once); the improvements of a hop are
+// applied in order at the start of the next (:282-291), and a vertex of Vh[h]
+// gets the label (hub, h, dist_hop) iff that distance is below the pruning
+// query at hop bound h (:304-336), and only then relaxes its neighbours
+// (:338-347).  hub_labels are the hub's labels from earlier hubs (its own
+// self label comes from hop 0 of this search).
+template <class LockScan, class Emit>
+void www_search(const Graph& g, int K, int hub, WwwScratch& S, const std::vector<Label>& hub_labels,
+                LockScan lock_scan, Emit emit, Index* stats) {
+  for (const Label& x : hub_labels) {
+    if (S.hubtab[x.hub].empty()) S.touched_hubs.push_back(x.hub);
+    S.hubtab[x.hub].push_back({x.dist, x.hop});
+  }
+  std::vector<std::vector<int32_t>> Vh((size_t)K + 2);
+  Vh[0].push_back(hub);
+  S.dist[hub] = 0;
+  S.pred[hub] = hub;
+  S.touched.push_back(hub);
+  struct Update {
+    int32_t v, d, p;
+  };
+  std::vector<Update> upd;
+  int64_t popped = 0, relaxed = 0, qreads = 0;
+  for (int h = 0; h <= K; h++) {
+    for (const Update& x : upd) {
+      if (S.dist[x.v] > x.d) {
+        if (S.dist[x.v] == INT_MAX) S.touched.push_back(x.v);
+        S.dist[x.v] = x.d;
+        S.pred[x.v] = x.p;
+      }
+    }
+    upd.clear();
+    for (int u : Vh[h]) {
+      popped++;
+      const int P_u = S.dist[u];
+      int q = INT_MAX;
+      lock_scan(u, [&](const std::vector<Label>& Lu) {
+        qreads += (int64_t)Lu.size();
+        for (const Label& xx : Lu) {
+          for (const auto& yy : S.hubtab[xx.hub]) {
+            if (xx.hop + yy.second <= h) {
+              long long d = (long long)xx.dist + yy.first;
+              if (q > d) q = (int)d;
+            }
+          }
+        }
+      });
+      if (!(P_u < q)) continue;
+      emit(u, Label{hub, S.pred[u], h, P_u});
+      for (int64_t e = g.rp[u]; e < g.rp[u + 1]; e++) {
+        const int v = g.col[e], nd = P_u + g.w[e];
+        relaxed++;
+        if (nd < S.dist[v]) {
+          Vh[h + 1].push_back(v);
+          upd.push_back({v, nd, u});
+        }
+      }
+    }
+  }
+  for (int v : S.touched) S.dist[v] = INT_MAX;
+  S.touched.clear();
+  for (int x : S.touched_hubs) S.hubtab[x].clear();
+  S.touched_hubs.clear();
+  if (stats) {
+    stats->popped += popped;
+    stats->relaxed += relaxed;
+    stats->query_reads += qreads;
+  }
+}
+
 void sort_all(Index& I) {
   for (auto& Lv : I.L) std::sort(Lv.begin(), Lv.end(), label_less);
 }
@@ -343,8 +425,10 @@ extern "C" {
 // wave_bounds/n_bounds: optional wave schedule (see header comment); when
 // given, generation is deterministic for any thread count.
 // clean: 0 none, 1 clean (mode chosen by threads: 1 -> mode 0, else mode 1).
+// variant: 0 HSDL_thread_function, 1 _2023WWW_thread_function (run with one
+// thread in rank order, or in wave mode with any thread count).
 void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, int K, int threads,
-                const int32_t* wave_bounds, int n_bounds, int clean) {
+                const int32_t* wave_bounds, int n_bounds, int clean, int variant) {
   Graph g{n, rp, col, w};
   Index* I = new Index();
   I->n = n;
@@ -352,7 +436,55 @@ void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, 
   I->L.assign(n, {});
   threads = std::max(1, threads);
   double t0 = now_s();
-  if (wave_bounds && n_bounds >= 2) {
+  const bool waves = wave_bounds && n_bounds >= 2;
+  if (variant == 1) {
+    std::vector<Index> stats(threads);
+    if (!waves) {
+      // rank order, labels visible as soon as they are written (generation.h:568-574 with one worker)
+      WwwScratch S(n);
+      std::vector<Label> snap;
+      for (int hub = 0; hub < n; hub++) {
+        snap = I->L[hub];
+        www_search(
+            g, K, hub, S, snap, [&](int u, auto fn) { fn(I->L[u]); },
+            [&](int u, const Label& x) { I->L[u].push_back(x); }, &stats[0]);
+      }
+    } else {
+      std::vector<std::vector<Label>> pending(n);
+      std::vector<std::mutex> mtx(n);
+      for (int b = 0; b + 1 < n_bounds; b++) {
+        int lo = wave_bounds[b], hi = wave_bounds[b + 1];
+        std::atomic<int> next{lo};
+        auto worker = [&](int tid) {
+          WwwScratch S(n);
+          for (;;) {
+            int hub = next.fetch_add(1);
+            if (hub >= hi) break;
+            www_search(
+                g, K, hub, S, I->L[hub], [&](int u, auto fn) { fn(I->L[u]); },
+                [&](int u, const Label& x) {
+                  std::lock_guard<std::mutex> lk(mtx[u]);
+                  pending[u].push_back(x);
+                },
+                &stats[tid]);
+          }
+        };
+        std::vector<std::thread> pool;
+        for (int i = 0; i < threads; i++) pool.emplace_back(worker, i);
+        for (auto& t : pool) t.join();
+        for (int v = 0; v < n; v++) {
+          if (pending[v].empty()) continue;
+          I->L[v].insert(I->L[v].end(), pending[v].begin(), pending[v].end());
+          pending[v].clear();
+        }
+      }
+    }
+    for (auto& st : stats) {
+      I->popped += st.popped;
+      I->relaxed += st.relaxed;
+      I->query_reads += st.query_reads;
+    }
+  } else if (waves) {
     // wave mode: every hub of a wave reads the labels of earlier waves only
     std::vector<std::vector<Label>> pending(n);
     std::vector<std::mutex> mtx(n);
@@ -443,7 +575,7 @@ void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, 
       I->query_reads += s.query_reads;
     }
   }
-  if (wave_bounds && n_bounds >= 2) {
+  if (variant != 1 && waves) {
     // in wave mode the self label is emitted by no search; add it per vertex
     // (the reference pushes it at the start of the hub's own search).
     for (int v = 0; v < n; v++) I->L[v].push_back(Label{v, v, 0, 0});

@@ -62,7 +62,7 @@ class Oracle:
         L = C.CDLL(path)
         vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
         L.orc_build.restype = vp
-        L.orc_build.argtypes = [i32, vp, vp, vp, i32, i32, vp, i32, i32]
+        L.orc_build.argtypes = [i32, vp, vp, vp, i32, i32, vp, i32, i32, i32]
         L.orc_from_labels.restype = vp
         L.orc_from_labels.argtypes = [i32, i32, vp, vp]
         L.orc_clean.argtypes = [vp, i32, i32]
@@ -95,13 +95,17 @@ class Oracle:
                                        "popped": int(work[0]), "relaxed": int(work[1]),
                                        "query_reads": int(work[2])})
 
-    def build(self, g, K: int, threads: int = 1, wave_bounds=None, clean: bool = True) -> Labels:
+    def build(self, g, K: int, threads: int = 1, wave_bounds=None, clean: bool = True,
+              www: bool = False) -> Labels:
         """Generation (+ sortL, + clean).  wave_bounds: the GPU's wave schedule
-        (hsdl_wave_bounds) to reproduce its uncleaned superset exactly."""
+        (hsdl_wave_bounds) to reproduce its uncleaned superset exactly.  www:
+        the reference's 2023WWW generation (one thread, or wave mode)."""
+        if www and wave_bounds is None and threads != 1:
+            raise ValueError("the 2023WWW generation runs with one thread or in wave mode")
         b = None if wave_bounds is None else np.ascontiguousarray(wave_bounds, np.int32)
         self._n = g.n
         h = self.L.orc_build(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), K, threads, _p(b),
-                             0 if b is None else len(b), int(clean))
+                             0 if b is None else len(b), int(clean), int(www))
         try:
             return self._export(h)
         finally:
@@ -153,7 +157,7 @@ class Reference:
         L = C.CDLL(path)
         vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
         L.ref_build.restype = C.c_int64
-        L.ref_build.argtypes = [i32, vp, vp, vp, i32, i32, i32]
+        L.ref_build.argtypes = [i32, vp, vp, vp, i32, i32, i32, i32]
         L.ref_times.argtypes = [vp]
         L.ref_export.argtypes = [vp, vp]
         L.ref_query.argtypes = [i64, vp, vp, vp, vp, i32]
@@ -163,8 +167,9 @@ class Reference:
         self.L = L
         self.n = 0
 
-    def build(self, g, K: int, threads: int = 1, clean: bool = True) -> Labels:
-        tot = self.L.ref_build(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), K, threads, int(clean))
+    def build(self, g, K: int, threads: int = 1, clean: bool = True, www: bool = False) -> Labels:
+        """www: the reference's 2023WWW generation instead of HSDL's."""
+        tot = self.L.ref_build(g.n, _p(g.row_ptr), _p(g.col), _p(g.w), K, threads, int(clean), int(www))
         self.n = g.n
         off = np.zeros(g.n + 1, np.int64)
         lab = np.zeros((max(1, tot), 4), np.int32)

@@ -49,14 +49,16 @@ void load_graph(int n, const int64_t* row_ptr, const int32_t* col, const int32_t
 extern "C" {
 
 // Runs generation (+ sortL, + canonical repair if `clean`) with the reference's
-// thread pool of `threads` workers.  Returns the total label count.
+// thread pool of `threads` workers; `www` selects the reference's 2023WWW
+// generation (_2023WWW_thread_function, hop_constrained_two_hop_labels_generation.h:226-370)
+// instead of HSDL_thread_function.  Returns the total label count.
 int64_t ref_build(int n, const int64_t* row_ptr, const int32_t* col, const int32_t* w, int K,
-                  int threads, int clean) {
+                  int threads, int clean, int www) {
   load_graph(n, row_ptr, col, w);
   hop_constrained_case_info mm;
   mm.upper_k = K;
   mm.use_rank_prune = 1;
-  mm.use_2023WWW_generation = 0;
+  mm.use_2023WWW_generation = www ? 1 : 0;
   mm.use_canonical_repair = clean ? 1 : 0;
   mm.thread_num = threads;
   hop_constrained_two_hop_labels_generation(g_graph, mm);

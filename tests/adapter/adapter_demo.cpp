@@ -9,6 +9,7 @@
 // every vertex, "ans <d>" per query (single-query calls) and "batch <d>" per
 // query (one batched call), "path <edges>" for the first query.
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "hsdl_reference_adapter.hpp"
@@ -25,6 +26,7 @@ struct graph_like {  // graph_v_of_v<int>: ADJs[v] = sorted (neighbour, weight) 
 
 struct case_like {  // hop_constrained_case_info
   int upper_k = 5;
+  bool use_2023WWW_generation = false;
   bool use_canonical_repair = true;
   double time_initialization = 0, time_generate_labels = 0, time_sortL = 0, time_canonical_repair = 0,
          time_total = 0;
@@ -33,7 +35,7 @@ struct case_like {  // hop_constrained_case_info
   std::vector<std::vector<label_like>> L;
 };
 
-int main() {
+int main(int argc, char** argv) {
   int n, m, K;
   if (std::scanf("%d %d %d", &n, &m, &K) != 3) return 2;
   graph_like g;
@@ -47,6 +49,7 @@ int main() {
   for (auto& row : g.ADJs) std::sort(row.begin(), row.end());
   case_like ci;
   ci.upper_k = K;
+  ci.use_2023WWW_generation = argc > 1 && std::strcmp(argv[1], "www") == 0;
   try {
     hsdl_gpu::hop_constrained_two_hop_labels_generation(g, ci);
     std::printf("labels %.0f %.0f\n", ci.label_size_before_canonical_repair, ci.label_size_after_canonical_repair);

@@ -64,3 +64,14 @@ def golden_cases():
 @pytest.fixture(params=golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
 def golden(request, built):
     return GoldenCase(request.param)
+
+
+def www_cases():
+    return sorted(glob.glob(os.path.join(GOLDEN, "www", "*.npz")))
+
+
+@pytest.fixture(params=www_cases(), ids=lambda p: "www_" + os.path.basename(p)[:-4])
+def golden_www(request, built):
+    """The reference's 2023WWW generation on a seeded graph: raw_off/raw_labels
+    before the clean, off/labels after (tests/golden/make_golden.py)."""
+    return GoldenCase(request.param)

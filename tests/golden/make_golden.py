@@ -61,6 +61,19 @@ def make(name: str, g, K: int, full: bool, nq: int = 4000, bf_sources: int = 20)
     print(f"{name}: n={g.n} m={g.num_edges} K={K} labels={len(lab.lab)} full={full}")
 
 
+def make_www(name: str, g, K: int):
+    """The reference's 2023WWW generation (use_2023WWW_generation = 1,
+    thread_num = 1): its labels before the clean (duplicates and parents
+    included, per vertex sorted) and after."""
+    R = O.Reference()
+    raw = R.build(g, K, threads=1, clean=False, www=True)
+    cln = R.build(g, K, threads=1, clean=True, www=True)
+    os.makedirs(os.path.join(OUT, "www"), exist_ok=True)
+    np.savez_compressed(os.path.join(OUT, "www", f"{name}.npz"), n=np.int32(g.n), K=np.int32(K), row_ptr=g.row_ptr,
+                        col=g.col, w=g.w, raw_off=raw.off, raw_labels=raw.lab, off=cln.off, labels=cln.lab)
+    print(f"www/{name}: n={g.n} m={g.num_edges} K={K} labels {len(raw.lab)} -> {len(cln.lab)}")
+
+
 def main():
     ref_dir = sys.argv[1] if len(sys.argv) > 1 else O.REF_DIR_DEFAULT
     O.build(ref_dir)
@@ -77,6 +90,10 @@ def main():
     make("cl_2000_k4", H.HostGraph.chung_lu(2000, 8, 2.2, 200, 1, 100, seed=6), 4, full=True)
     make("ba_800_k6", H.HostGraph.barabasi_albert(800, 3, 1, 1000, seed=7), 6, full=True)
     make("er_300_unit_k3", H.HostGraph.erdos_renyi(300, 900, 1, 1, seed=8), 3, full=True)
+    # the 2023WWW generation (generation.h:226-370)
+    make_www("er_150_600_k4", H.HostGraph.erdos_renyi(150, 600, 1, 100, seed=9), 4)
+    make_www("er_300_unit_k3", H.HostGraph.erdos_renyi(300, 900, 1, 1, seed=8), 3)
+    make_www("cl_600_k5", H.HostGraph.chung_lu(600, 6, 2.2, 80, 1, 100, seed=10), 5)
 
 
 if __name__ == "__main__":

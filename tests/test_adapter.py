@@ -34,7 +34,10 @@ def test_adapter_binds_to_the_reference_types():
 
 
 @pytest.mark.gpu
-def test_adapter_program_matches_the_c_abi(tmp_path):
+@pytest.mark.parametrize("www", [False, True])
+def test_adapter_program_matches_the_c_abi(tmp_path, www):
+    """www: case_info.use_2023WWW_generation = true (the 2023WWW search);
+    more labels before the clean, the same labels after it."""
     exe = str(tmp_path / "adapter_demo")
     cmd = ["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
            os.path.join(HERE, "adapter", "adapter_demo.cpp"), "-L" + LIBDIR, "-lhsdl",
@@ -51,14 +54,17 @@ def test_adapter_program_matches_the_c_abi(tmp_path):
     k = rng.integers(0, K + 1, q).astype(np.int32)
     lines = [f"{g.n} {len(a)} {K}"] + [f"{x} {y} {z}" for x, y, z in zip(a, b, w)] + [str(q)]
     lines += [f"{x} {y} {z}" for x, y, z in zip(s, t, k)]
-    r = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True)
+    r = subprocess.run([exe] + (["www"] if www else []), input="\n".join(lines) + "\n", capture_output=True,
+                       text=True)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     out = r.stdout.split("\n")
-    idx = H.Index.build(H.Graph(g), K)
+    idx = H.Index.build(H.Graph(g), K, generation=1 if www else 0)
     info = idx.info()
     off, _ = idx.export()
     before, after = next(l for l in out if l.startswith("labels")).split()[1:]
     assert int(before) == info["labels_before_clean"] and int(after) == info["labels"]
+    if www:
+        assert info["labels"] == H.Index.build(H.Graph(g), K).info()["labels"]
     rows = np.array([int(l.split()[2]) for l in out if l.startswith("row ")])
     assert np.array_equal(rows, np.diff(off))
     want = idx.query(s, t, k)
