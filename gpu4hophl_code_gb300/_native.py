@@ -48,7 +48,7 @@ class hsdl_index_info(C.Structure):
                 ("device_bytes", C.c_int64), ("time_generate_s", C.c_double), ("time_sort_s", C.c_double),
                 ("time_clean_s", C.c_double), ("max_row", C.c_int64), ("work_relaxations", C.c_int64),
                 ("work_join_reads", C.c_int64), ("work_labels_written", C.c_int64), ("work_clean_reads", C.c_int64),
-                ("work_candidates", C.c_int64),
+                ("work_candidates", C.c_int64), ("work_join_visible", C.c_int64),
                 ("build_peak_bytes", C.c_int64), ("build_pool_entries", C.c_int64),
                 ("build_max_candidates", C.c_int64), ("build_wave_splits", C.c_int32), ("build_pool_chunks", C.c_int32)]
 

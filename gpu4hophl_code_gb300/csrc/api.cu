@@ -596,6 +596,7 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->work_labels_written = idx->work_labels_written;
   info->work_clean_reads = idx->work_clean_reads;
   info->work_candidates = idx->work_candidates;
+  info->work_join_visible = idx->work_join_visible;
   info->build_peak_bytes = idx->build_peak;
   info->build_pool_entries = idx->build_pool;
   info->build_max_candidates = idx->build_max_cand;

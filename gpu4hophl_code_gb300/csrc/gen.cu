@@ -125,6 +125,7 @@ struct Counters {
   unsigned long long touched;     // rows receiving labels this wave
   unsigned long long relax;       // relaxations this wave (work counter)
   unsigned long long reads;       // committed labels read by the pruning join (work counter)
+  unsigned long long visible;     // committed labels of the joined candidates' rows (work counter)
   unsigned long long hop_c[16];   // candidate-list start of each hop
   unsigned long long hop_f[16];   // frontier size of each hop
   unsigned long long seg_need;     // pool entries of the segments this commit adds
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
   const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (gi * G));
   const int32_t s_hub = ctr->s_hub;
   const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
-  unsigned long long scanned = 0;
+  unsigned long long scanned = 0, visible = 0;
   for (;;) {
     unsigned long long took = 0;
     if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(8 * NG));
@@ -392,6 +393,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         const uint32_t theta = (uint32_t)tab_theta[slot];
         uint32_t mask = (uint32_t)cap - 1;
         int len = row_len[v];
+        visible += (unsigned long long)len;
         // lane gl of the group holds the address of the row's segment gl, so
         // a label's address takes a shuffle instead of two dependent loads
         const uint64_t* my_seg = nullptr;
@@ -491,6 +493,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
     }
   }
   if (gl == 0 && scanned) atomicAdd(&ctr->reads, scanned);
+  if (gl == 0 && visible) atomicAdd(&ctr->visible, visible);
 }
 
 // ---------------------------------------------------------------------------
@@ -980,6 +983,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     idx->work_relax += (int64_t)hc.relax;
     idx->work_candidates += (int64_t)std::min<unsigned long long>(hc.c_count, (unsigned long long)capC);
     idx->work_join_reads += (int64_t)hc.reads;
+    idx->work_join_visible += (int64_t)hc.visible;
     idx->work_labels_written += (int64_t)hc.wl_count;
     // commit the wave's labels
     if (hc.wl_count > 0) {

@@ -117,6 +117,7 @@ struct hsdl_index_impl {
   double t_gen = 0, t_sort = 0, t_clean = 0;
   // work counted on the device during the build (for the roofline)
   int64_t work_relax = 0, work_join_reads = 0, work_labels_written = 0, work_clean_reads = 0, work_candidates = 0;
+  int64_t work_join_visible = 0;
   // device memory of the build
   int64_t build_peak = 0, build_pool = 0, build_max_cand = 0;
   int32_t wave_splits = 0, pool_chunks = 0;

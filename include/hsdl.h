@@ -263,6 +263,8 @@ typedef struct hsdl_index_info {
   int64_t work_labels_written;   /* labels generated (before clean) */
   int64_t work_clean_reads;      /* labels read by the clean's joins */
   int64_t work_candidates;       /* (hub, vertex) candidates the pruning joins decided */
+  int64_t work_join_visible;     /* committed labels in the rows of those candidates (what a join without
+                                    early exit reads; the joins stop at a dominating label) */
   /* device memory of the build */
   int64_t build_peak_bytes;      /* most HBM the build's buffers held at once */
   int64_t build_pool_entries;    /* label-pool entries the generation's rows occupied (labels and row slack) */
