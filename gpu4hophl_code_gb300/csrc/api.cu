@@ -76,17 +76,6 @@ int new_index(hsdl_index** out) {
     set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     return HSDL_ERR_CUDA;
   }
-  // the query kernels' error word, allocated here so that no query call allocates
-  int rc = idx->qerr.alloc(1, idx->stream);
-  if (rc == HSDL_OK && cudaMemsetAsync(idx->qerr.p, 0, sizeof(unsigned int), idx->stream) != cudaSuccess)
-    rc = HSDL_ERR_CUDA;
-  if (rc == HSDL_OK && cudaStreamSynchronize(idx->stream) != cudaSuccess) rc = HSDL_ERR_CUDA;
-  if (rc != HSDL_OK) {
-    cudaStreamDestroy(idx->stream);
-    delete idx;
-    set_error("query error word allocation failed");
-    return rc;
-  }
   *out = idx;
   return HSDL_OK;
 }
@@ -97,7 +86,6 @@ void free_index(hsdl_index* idx) {
   idx->off.release();
   idx->key.release();
   idx->par.release();
-  idx->qerr.release();
   idx->wave_lo.release();
   if (idx->stream) {
     cudaStreamSynchronize(idx->stream);
@@ -504,7 +492,6 @@ int hsdl_query_batch(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_
     set_error("query vertex out of range at query " + std::to_string(first));
     return HSDL_ERR_INVALID;
   }
-  if (rc == HSDL_OK) rc = query_error(idx);
   return rc;
 }
 

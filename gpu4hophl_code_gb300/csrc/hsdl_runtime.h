@@ -106,7 +106,6 @@ struct hsdl_index_impl {
   DevBuf<int64_t> off;    // n+1
   DevBuf<uint64_t> key;   // hub:32 | hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
-  DevBuf<unsigned int> qerr;  // set by a query kernel whose bounded wait ran out
   DevBuf<int32_t> wave_lo;    // generated, not yet cleaned: first hub of each hub's wave
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
@@ -165,7 +164,6 @@ int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
 // smallest index of a query with s or t outside [0, n), all-ones if none.
 int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, unsigned long long* d_first,
                     cudaStream_t st);
-int query_error(hsdl_index_impl* idx);  // HSDL_ERR_TIMEOUT (and clears) if a query kernel flagged one
 int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int64_t max_row, cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total
 

@@ -102,16 +102,4 @@ int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
   }
 }
 
-int query_error(hsdl_index_impl* idx) {
-  if (!idx->qerr.p) return HSDL_OK;
-  unsigned int e = 0;
-  HSDL_CUDA(cudaMemcpy(&e, idx->qerr.p, sizeof(e), cudaMemcpyDeviceToHost));
-  if (e) {
-    HSDL_CUDA(cudaMemset(idx->qerr.p, 0, sizeof(e)));
-    set_error("a bounded wait for staged label rows ran out in the query kernel");
-    return HSDL_ERR_TIMEOUT;
-  }
-  return HSDL_OK;
-}
-
 }  // namespace hsdl

@@ -28,7 +28,7 @@ extern "C" {
 #define HSDL_ERR_INVALID 1 /* bad argument or malformed input */
 #define HSDL_ERR_CUDA 2    /* CUDA runtime failure (no device, launch error) */
 #define HSDL_ERR_NOMEM 3   /* allocation failed or over the caller's budget */
-#define HSDL_ERR_TIMEOUT 4 /* a bounded device-side wait ran out */
+#define HSDL_ERR_TIMEOUT 4 /* a bounded wait ran out (hsdl_serve_wait, hsdl_serve_wait_graph, the loop draining) */
 #define HSDL_ERR_STATE 5   /* call not valid in the handle's current state */
 #define HSDL_ERR_FULL 6    /* a queue or slot table is full */
 #define HSDL_ERR_IO 7      /* file could not be read or written */

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import gpu4hophl_code_gb300 as H
-from gpu4hophl_code_gb300._native import HSDL_ERR_FULL, HsdlError
+from gpu4hophl_code_gb300._native import HSDL_ERR_FULL, HSDL_ERR_TIMEOUT, HsdlError
 
 pytestmark = pytest.mark.gpu
 
@@ -93,6 +93,9 @@ def test_idle_exit_relaunch_bad_ids_and_removal():
     s, t, k = _queries(rng, g.n, 5000, K)
     a1 = srv.query(np.full(5000, gid, np.int32), s, t, k)
     time.sleep(0.3)  # the loop returns after 50 ms idle
+    st = srv.stats()
+    assert st["loop_running"] == 0  # its bounded idle wait ran out and it returned
+    assert st["processed"] == st["submitted"] == 5000
     a2 = srv.query(np.full(5000, gid, np.int32), s, t, k)  # relaunched
     assert np.array_equal(a1, a2) and np.array_equal(a1, ix.query(s, t, k))
     bad = srv.query(np.array([gid + 7, -1], np.int32), s[:2], t[:2], k[:2])
@@ -111,4 +114,23 @@ def test_build_admission_budget():
     with pytest.raises(HsdlError) as e:
         srv.submit_build(dev, 5)
     assert e.value.code == HSDL_ERR_FULL and "budget" in str(e.value)
+    srv.close()
+
+
+def test_wait_that_runs_out_reports_timeout():
+    """A bounded wait that runs out returns HSDL_ERR_TIMEOUT and leaves the
+    server usable: waiting no time at all for a build that has just been
+    queued."""
+    g = H.HostGraph.chung_lu(200000, 8, 2.2, 2000, 1, 100, seed=71)
+    dev = H.Graph(g)
+    srv = H.Server(idle_exit_s=0.05)
+    gid = srv.submit_build(dev, 5)
+    with pytest.raises(HsdlError) as e:
+        srv.wait_graph(gid, timeout_s=0.0)
+    assert e.value.code == HSDL_ERR_TIMEOUT
+    srv.wait_graph(gid, timeout_s=600.0)
+    rng = np.random.default_rng(9)
+    s, t, k = _queries(rng, g.n, 20000, 5)
+    ref = H.Index.build(dev, 5)
+    assert np.array_equal(srv.query(np.full(20000, gid, np.int32), s, t, k), ref.query(s, t, k))
     srv.close()
