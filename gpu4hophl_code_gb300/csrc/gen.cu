@@ -132,6 +132,8 @@ struct Counters {
   unsigned long long seg_over;     // a row would need more than kSegs segments
   unsigned long long take_e[16];  // expansion tiles taken (dynamic work distribution)
   unsigned long long take_p[16];  // pruning candidates taken
+  unsigned long long heavy_chunks[16];  // chunks of heavy expansion tiles in the chunk map
+  unsigned long long take_h[16];        // heavy chunks taken
   int s_hub;                      // first hub of the wave (read by the captured hop kernels)
   int pad32;
 };
@@ -257,24 +259,111 @@ __global__ void k_table_prefix(const Counters* ctr, int32_t* __restrict__ tab, i
 // ---------------------------------------------------------------------------
 // hop round: expansion
 // ---------------------------------------------------------------------------
+// Relaxations of one heavy tile per chunk of the expansion's second kernel,
+// and the tile size (in relaxations) above which a tile is split that way.
+constexpr int64_t kExpandChunk = 8192;
+constexpr int64_t kExpandHeavy = 2 * kExpandChunk;
+constexpr int64_t kExpandChunkCap = 1 << 20;  // chunk-map entries (8 MB); past it tiles run whole
+
+template <int TPB>
+struct ExpandTile {
+  int64_t start[TPB];
+  int64_t lo[TPB];
+  int4 e[TPB];
+  int64_t scan[32];
+};
+
+// Loads frontier tile `tile` into the block's shared arrays: per entry its
+// relaxation count (with rank_prune the suffix of its row after the hub's id,
+// found by binary search; otherwise the whole row) and the exclusive scan of
+// the counts.  Returns the tile's relaxations (every thread).
+template <int TPB>
+__device__ inline int64_t expand_tile_setup(ExpandTile<TPB>& t, SlotMap map, int32_t h, int32_t K, int32_t rank_prune,
+                                            int64_t tile, int64_t nf, int32_t s_hub, const int64_t* __restrict__ rp,
+                                            const int2* __restrict__ adj, const int4* __restrict__ F) {
+  const int64_t i = tile * TPB + threadIdx.x;
+  int64_t len = 0, lo = 0;
+  int4 e = make_int4(0, 0, 0, 0);
+  if (i < nf && h <= map.hop_bound(s_hub + F[i].x, K)) {
+    e = F[i];
+    const int hub = s_hub + e.x;
+    lo = rp[e.y];
+    const int64_t hi = rp[e.y + 1];
+    if (rank_prune) {
+      int64_t a = lo, b = hi;
+      while (a < b) {
+        const int64_t mid = (a + b) >> 1;
+        if (adj[mid].x <= hub) a = mid + 1; else b = mid;
+      }
+      lo = a;
+    }
+    len = hi - lo;
+  }
+  int64_t total;
+  const int64_t pre = block_exclusive_scan(len, t.scan, &total);
+  t.start[threadIdx.x] = pre;
+  t.lo[threadIdx.x] = lo;
+  t.e[threadIdx.x] = e;
+  __syncthreads();
+  return total;
+}
+
+// Relaxations [j0, j1) of the tile in shared memory, spread over the block:
+// atomicMin on the candidate key keeps the best (distance, hop, parent), and
+// the first improvement of a (slot, v) in this hop appends it to the
+// candidate list.
+template <int TPB>
+__device__ inline void expand_relax(const ExpandTile<TPB>& t, SlotMap map, int32_t h, int64_t j0, int64_t j1,
+                                    const int2* __restrict__ adj, uint64_t* __restrict__ cand,
+                                    int2* __restrict__ C, int64_t capC, Counters* ctr, int2* wbuf, int& wn) {
+  const int lane = lane_id();
+  // warp-uniform trip count: lanes past j1 stage nothing
+  for (int64_t jw = j0 + (int64_t)(threadIdx.x - lane); jw < j1; jw += TPB) {
+    const int64_t j = jw + lane;
+    bool app = false;
+    int2 entry = make_int2(0, 0);
+    if (j < j1) {
+      int a = 0, b = TPB - 1;
+      while (a < b) {
+        const int mid = (a + b + 1) >> 1;
+        if (t.start[mid] <= j) a = mid; else b = mid - 1;
+      }
+      const int4 oe = t.e[a];
+      const int2 nb = adj[t.lo[a] + (j - t.start[a])];
+      const uint64_t key = ckey((uint32_t)oe.z + (uint32_t)nb.y, (uint32_t)h, (uint32_t)oe.y);
+      uint64_t* p = cand + map.row(oe.x) + map.local(nb.x);
+      if (key < __ldcg((const unsigned long long*)p)) {
+        const uint64_t old = atomicMin((unsigned long long*)p, (unsigned long long)key);
+        app = key < old && ckey_hop(old) != (uint32_t)h;
+      }
+      entry = make_int2(oe.x, nb.x);
+    }
+    warp_stage(wbuf, wn, app, entry, &ctr->c_count, C, capC, &ctr->overflow);
+  }
+}
+
 // Each block takes `tiles` tiles of TPB frontier entries at a time from a
-// per-hop counter, so a block that drew heavy vertices takes fewer tiles.
-// With rank_prune (the HSDL search) only neighbours ranked below the hub are
-// relaxed (generation.h:107-110); rows are sorted by neighbour id, so they
-// are the suffix after the hub's id, found by binary search.  Without it (the
-// 2023WWW search, generation.h:338-347) every neighbour is relaxed.  The
-// tile's relaxations are spread evenly over the block through an exclusive
-// scan of the row lengths.
+// per-hop counter and relaxes them.  With rank_prune (the HSDL search) only
+// neighbours ranked below the hub are relaxed (generation.h:107-110); without
+// it (the 2023WWW search, generation.h:338-347) every neighbour is.  A tile
+// with more than kExpandHeavy relaxations is not relaxed here: its chunks of
+// kExpandChunk relaxations go to the chunk map for k_expand_heavy, which
+// spreads them over all blocks.  (A block relaxing a whole heavy tile set
+// the launch's time alone: the first hop's frontier is the wave's hubs, 256
+// consecutive ranks of similar degree per tile, so a wave of 4,375 hubs kept
+// 17 blocks busy, and an ncu capture of one expansion showed one SM active
+// for 1.49 M cycles against 13 K on average.)
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t K, int32_t rank_prune, int32_t tiles,
                                                 const int64_t* __restrict__ rp, const int2* __restrict__ adj,
                                                 const int4* __restrict__ F, uint64_t* __restrict__ cand,
-                                                int2* __restrict__ C, int64_t capC, Counters* ctr) {
-  __shared__ int64_t s_start[TPB];
-  __shared__ int64_t s_lo[TPB];
-  __shared__ int4 s_e[TPB];
-  __shared__ int64_t s_scan[32];
-  __shared__ int64_t s_tile;
+                                                int2* __restrict__ C, int64_t capC, Counters* ctr,
+                                                int2* __restrict__ chunk_map) {
+  __shared__ ExpandTile<TPB> t;
+  __shared__ int64_t s_tile, s_defer;
+  __shared__ int2 s_stage[TPB / 32][64];  // per-warp staging of candidate-list appends
+  int2* wbuf = s_stage[threadIdx.x >> 5];
+  int wn = 0;
   const int32_t s_hub = ctr->s_hub;
   const int64_t nf = (int64_t)ctr->hop_f[h - 1];
   for (;;) {
@@ -283,55 +372,61 @@ __global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t 
     const int64_t first = s_tile;
     if (first * TPB >= nf) break;
     for (int64_t tile = first; tile < first + tiles && tile * TPB < nf; tile++) {
-      int64_t i = tile * TPB + threadIdx.x;
-      int64_t len = 0, lo = 0;
-      int4 e = make_int4(0, 0, 0, 0);
-      if (i < nf && h <= map.hop_bound(s_hub + F[i].x, K)) {
-        e = F[i];
-        int hub = s_hub + e.x;
-        lo = rp[e.y];
-        int64_t hi = rp[e.y + 1];
-        if (rank_prune) {
-          int64_t a = lo, b = hi;
-          while (a < b) {
-            int64_t mid = (a + b) >> 1;
-            if (adj[mid].x <= hub) a = mid + 1; else b = mid;
-          }
-          lo = a;
-        }
-        len = hi - lo;
-      }
-      int64_t total;
-      int64_t pre = block_exclusive_scan(len, s_scan, &total);
+      const int64_t total = expand_tile_setup(t, map, h, K, rank_prune, tile, nf, s_hub, rp, adj, F);
       if (threadIdx.x == 0 && total) atomicAdd(&ctr->relax, (unsigned long long)total);
-      s_start[threadIdx.x] = pre;
-      s_lo[threadIdx.x] = lo;
-      s_e[threadIdx.x] = e;
-      __syncthreads();
-      for (int64_t j = threadIdx.x; j < total; j += TPB) {
-        int a = 0, b = TPB - 1;
-        while (a < b) {
-          int mid = (a + b + 1) >> 1;
-          if (s_start[mid] <= j) a = mid; else b = mid - 1;
+      if (total > kExpandHeavy) {
+        const int64_t nch = (total + kExpandChunk - 1) / kExpandChunk;
+        if (threadIdx.x == 0) {
+          const int64_t c0 = (int64_t)atomicAdd(&ctr->heavy_chunks[h], (unsigned long long)nch);
+          s_defer = c0 + nch <= kExpandChunkCap ? c0 : -1 - c0;
         }
-        int4 oe = s_e[a];
-        int2 nb = adj[s_lo[a] + (j - s_start[a])];
-        uint64_t key = ckey((uint32_t)oe.z + (uint32_t)nb.y, (uint32_t)h, (uint32_t)oe.y);
-        uint64_t* p = cand + map.row(oe.x) + map.local(nb.x);
-        bool app = false;
-        if (key < __ldcg((const unsigned long long*)p)) {
-          uint64_t old = atomicMin((unsigned long long*)p, (unsigned long long)key);
-          app = key < old && ckey_hop(old) != (uint32_t)h;
+        __syncthreads();
+        const int64_t d = s_defer;
+        if (d >= 0) {
+          for (int64_t q = threadIdx.x; q < nch; q += TPB) chunk_map[d + q] = make_int2((int)tile, (int)q);
+          __syncthreads();
+          continue;
         }
-        long long pos = warp_append(app, &ctr->c_count);
-        if (app) {
-          if (pos < capC) C[pos] = make_int2(oe.x, nb.x);
-          else ctr->overflow = 1;
-        }
+        // the map is full: mark this tile's entries in it as done and relax it here
+        for (int64_t c = -1 - d + threadIdx.x; c < kExpandChunkCap; c += TPB) chunk_map[c] = make_int2(-1, 0);
       }
+      expand_relax(t, map, h, 0, total, adj, cand, C, capC, ctr, wbuf, wn);
       __syncthreads();
     }
   }
+  warp_stage_flush(wbuf, wn, &ctr->c_count, C, capC, &ctr->overflow);
+}
+
+// The chunks of the heavy tiles k_expand deferred: each block takes a chunk,
+// rebuilds its tile's scan and relaxes the chunk's kExpandChunk relaxations.
+template <int TPB>
+__global__ void __launch_bounds__(TPB) k_expand_heavy(SlotMap map, int32_t h, int32_t K, int32_t rank_prune,
+                                                      const int64_t* __restrict__ rp, const int2* __restrict__ adj,
+                                                      const int4* __restrict__ F, uint64_t* __restrict__ cand,
+                                                      int2* __restrict__ C, int64_t capC, Counters* ctr,
+                                                      const int2* __restrict__ chunk_map) {
+  __shared__ ExpandTile<TPB> t;
+  __shared__ int64_t s_chunk;
+  __shared__ int2 s_stage[TPB / 32][64];
+  int2* wbuf = s_stage[threadIdx.x >> 5];
+  int wn = 0;
+  const int32_t s_hub = ctr->s_hub;
+  const int64_t nf = (int64_t)ctr->hop_f[h - 1];
+  const int64_t nch = min((int64_t)ctr->heavy_chunks[h], kExpandChunkCap);
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = (int64_t)atomicAdd(&ctr->take_h[h], 1ull);
+    __syncthreads();
+    const int64_t c = s_chunk;
+    __syncthreads();
+    if (c >= nch) break;
+    const int2 m = chunk_map[c];
+    if (m.x < 0) continue;
+    const int64_t total = expand_tile_setup(t, map, h, K, rank_prune, (int64_t)m.x, nf, s_hub, rp, adj, F);
+    const int64_t j0 = (int64_t)m.y * kExpandChunk;
+    expand_relax(t, map, h, j0, min(j0 + kExpandChunk, total), adj, cand, C, capC, ctr, wbuf, wn);
+    __syncthreads();
+  }
+  warp_stage_flush(wbuf, wn, &ctr->c_count, C, capC, &ctr->overflow);
 }
 
 // Closes hop h's candidate range.  On overflow the range stops at the list's
@@ -351,6 +446,38 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
 // read G labels of v at a time and stop as soon as one dominates.  Warps take
 // 8 candidates per group at a time from a per-hop counter, so candidates with
 // long label lists do not hold back a statically assigned share.
+// Moves a warp's staged kept candidates (slot, v, d, parent) to the wave's
+// found-label lists, and those below their hub's hop bound to the next
+// frontier: one atomic per list per 32 entries.  Every lane calls it.
+__device__ inline void prune_flush(int4* kbuf, int& kn, SlotMap map, int32_t h, int32_t K, int32_t s_hub,
+                                   int4* __restrict__ Fout, int32_t* __restrict__ wl_v,
+                                   uint64_t* __restrict__ wl_key, int32_t* __restrict__ wl_par, Counters* ctr) {
+  __syncwarp();
+  const int lane = lane_id();
+  unsigned long long base = 0;
+  if (lane == 0 && kn > 0) base = atomicAdd(&ctr->wl_count, (unsigned long long)kn);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int jb = 0; jb < kn; jb += 32) {
+    const int j = jb + lane;
+    const bool valid = j < kn;
+    const int4 x = valid ? kbuf[j] : make_int4(0, 0, 0, 0);
+    if (valid) {
+      const unsigned long long p = base + (unsigned long long)j;
+      wl_v[p] = x.y;
+      wl_key[p] = lkey((uint32_t)(s_hub + x.x), (uint32_t)h, (uint32_t)x.z);
+      wl_par[p] = x.w;
+    }
+    const bool fr = valid && h < map.hop_bound(s_hub + x.x, K);
+    const unsigned fm = __ballot_sync(0xffffffffu, fr);
+    unsigned long long fb = 0;
+    if (lane == 0 && fm) fb = atomicAdd(&ctr->hop_f[h], (unsigned long long)__popc(fm));
+    fb = __shfl_sync(0xffffffffu, fb, 0);
+    if (fr) Fout[fb + __popc(fm & ((1u << lane) - 1u))] = make_int4(x.x, x.y, x.z, 0);
+  }
+  __syncwarp();
+  kn = 0;
+}
+
 template <int G, int P, bool SELF = false>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
@@ -370,6 +497,9 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
   const int32_t s_hub = ctr->s_hub;
   const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
   unsigned long long scanned = 0, visible = 0;
+  __shared__ int4 s_kept[kThreads / 32][64];  // per-warp staging of kept candidates: slot, v, d, parent
+  int4* kbuf = s_kept[threadIdx.x >> 5];
+  int kn = 0;
   for (;;) {
     unsigned long long took = 0;
     if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(8 * NG));
@@ -380,7 +510,12 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
     // (Loading the set-up of a group's 8 candidates up front, one lane each,
     // doubled the registers of the 32-lane kernel and halved its occupancy:
     // generation went from 2.28 s to 2.83 s at n = 1M.)
-    for (int64_t i = i0 + gi; i < i1; i += NG) {
+    // warp-uniform trip count: a group past i1 decides nothing but stages with the warp
+    for (int64_t ib = i0; ib < i1; ib += NG) {
+      const int64_t i = ib + gi;
+      bool keep = false;
+      int4 kept = make_int4(0, 0, 0, 0);
+      if (i < i1) {
       int2 e = C[i];
       int slot = e.x, v = e.y;
       uint64_t ck = cand[map.row(slot) + map.local(v)];
@@ -480,18 +615,18 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
           q = x < q ? x : q;
         }
       }
-      if (d < q && gl == 0) {
-        unsigned long long p = atomicAdd(&ctr->wl_count, 1ull);
-        wl_v[p] = v;
-        wl_key[p] = lkey((uint32_t)(s_hub + slot), (uint32_t)h, (uint32_t)d);
-        wl_par[p] = (int32_t)ckey_parent(ck);
-        if (h < map.hop_bound(s_hub + slot, K)) {
-          unsigned long long f = atomicAdd(&ctr->hop_f[h], 1ull);
-          Fout[f] = make_int4(slot, v, (int)d, 0);
-        }
+      keep = d < q && gl == 0;
+      kept = make_int4(slot, v, (int)d, (int32_t)ckey_parent(ck));
       }
+      // kept candidates become labels (and the next frontier) through the
+      // warp's staging buffer: one atomic per 32 or more labels
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (keep) kbuf[kn + __popc(m & ((1u << lane) - 1u))] = kept;
+      kn += __popc(m);
+      if (kn >= 32) prune_flush(kbuf, kn, map, h, K, s_hub, Fout, wl_v, wl_key, wl_par, ctr);
     }
   }
+  prune_flush(kbuf, kn, map, h, K, s_hub, Fout, wl_v, wl_key, wl_par, ctr);
   if (gl == 0 && scanned) atomicAdd(&ctr->reads, scanned);
   if (gl == 0 && visible) atomicAdd(&ctr->visible, visible);
 }
@@ -833,6 +968,11 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   const int g_expand = sms * (tpb == 128   ? resident_blocks(k_expand<128>, 128)
                               : tpb == 512 ? resident_blocks(k_expand<512>, 512)
                                            : resident_blocks(k_expand<256>, 256));
+  const int g_heavy = sms * (tpb == 128   ? resident_blocks(k_expand_heavy<128>, 128)
+                             : tpb == 512 ? resident_blocks(k_expand_heavy<512>, 512)
+                                          : resident_blocks(k_expand_heavy<256>, 256));
+  DevBuf<int2> chunk_map;  // heavy expansion tiles, split into chunks
+  HSDL_TRY(chunk_map.alloc(kExpandChunkCap, st));
   const int pairs = opts.prune_pairs == 2 ? 2 : 1;
   const int g_prune8 = sms * (!rank_prune ? resident_blocks(k_prune<8, 1, true>, kThreads)
                               : pairs == 2 ? resident_blocks(k_prune<8, 2>, kThreads)
@@ -852,7 +992,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     return cand.bytes() + row_len.bytes() + cnt.bytes() + touched.bytes() + seg.bytes() +
            pool_total * kPoolEntryBytes + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
            wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() +
-           filt.bytes() + idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
+           filt.bytes() + chunk_map.bytes() + idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
   };
   auto note_peak = [&]() { idx->build_peak = std::max(idx->build_peak, held()); };
   note_peak();
@@ -865,12 +1005,20 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     for (int32_t h = 1; h <= K; h++) {
       int4* Fin = (h & 1) ? Fa.p : Fb.p;
       int4* Fout = (h & 1) ? Fb.p : Fa.p;
-      if (tpb == 128)
-        k_expand<128><<<g_expand, 128, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
-      else if (tpb == 512)
-        k_expand<512><<<g_expand, 512, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
-      else
-        k_expand<256><<<g_expand, 256, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, capC, ctr.p);
+#define HSDL_EXPAND(TPB)                                                                                  \
+  k_expand<TPB><<<g_expand, TPB, 0, st>>>(map, h, K, rank_prune, tiles, g->rp.p, g->adj.p, Fin, cand.p, Cl.p, \
+                                          capC, ctr.p, chunk_map.p);                                         \
+  HSDL_CUDA(cudaGetLastError());                                                                            \
+  k_expand_heavy<TPB><<<g_heavy, TPB, 0, st>>>(map, h, K, rank_prune, g->rp.p, g->adj.p, Fin, cand.p, Cl.p,  \
+                                               capC, ctr.p, chunk_map.p)
+      if (tpb == 128) {
+        HSDL_EXPAND(128);
+      } else if (tpb == 512) {
+        HSDL_EXPAND(512);
+      } else {
+        HSDL_EXPAND(256);
+      }
+#undef HSDL_EXPAND
       HSDL_CUDA(cudaGetLastError());
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());

@@ -102,6 +102,39 @@ __device__ inline long long warp_append(bool pred, unsigned long long* counter) 
   return (long long)(base + __popc(ballot & ((1u << lane) - 1)));
 }
 
+// Per-warp staging of list appends.  Lanes with an entry put it in the
+// warp's shared-memory buffer (64 entries); once the buffer holds 32 or more,
+// the warp moves it to the global list with a single atomic on the list's
+// counter.  Many warps appending one entry each to the same counter
+// serialise on the one L2 slice that holds it; staging cuts those atomics by
+// the buffer's fill.  Every lane of the warp must call these (convergent);
+// `n` is warp-uniform.
+template <class T>
+__device__ inline void warp_stage_flush(T* buf, int& n, unsigned long long* counter, T* out, int64_t cap,
+                                        unsigned long long* overflow) {
+  __syncwarp();
+  const int lane = lane_id();
+  unsigned long long base = 0;
+  if (lane == 0 && n > 0) base = atomicAdd(counter, (unsigned long long)n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int j = lane; j < n; j += 32) {
+    const unsigned long long p = base + (unsigned long long)j;
+    if ((int64_t)p < cap) out[p] = buf[j];
+    else *overflow = 1;
+  }
+  __syncwarp();
+  n = 0;
+}
+
+template <class T>
+__device__ inline void warp_stage(T* buf, int& n, bool pred, const T& val, unsigned long long* counter, T* out,
+                                  int64_t cap, unsigned long long* overflow) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if (pred) buf[n + __popc(m & ((1u << lane_id()) - 1u))] = val;
+  n += __popc(m);
+  if (n >= 32) warp_stage_flush(buf, n, counter, out, cap, overflow);
+}
+
 // Block-wide exclusive scan of one int64 per thread (blockDim.x <= 1024,
 // multiple of 32).  `smem` must hold 32 int64.  Returns the exclusive prefix;
 // *total receives the block sum.
