@@ -478,6 +478,10 @@ __device__ inline void prune_flush(int4* kbuf, int& kn, SlotMap map, int32_t h, 
   kn = 0;
 }
 
+// Candidates a lane group takes at a time from the hop's counter: 2 / 4 / 8 /
+// 32 gave generation 1.95 / 1.92 / 1.93 / 2.05 s at n = 1M (larger takes
+// leave a longer tail, smaller ones contend on the counter).
+constexpr int kPruneTake = 4;
 template <int G, int P, bool SELF = false>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
@@ -502,11 +506,11 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
   int kn = 0;
   for (;;) {
     unsigned long long took = 0;
-    if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(8 * NG));
+    if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(kPruneTake * NG));
     took = __shfl_sync(0xffffffffu, took, 0);
     const int64_t i0 = c0 + (int64_t)took;
     if (i0 >= c1) break;
-    const int64_t i1 = min(c1, i0 + 8 * NG);
+    const int64_t i1 = min(c1, i0 + kPruneTake * NG);
     // (Loading the set-up of a group's 8 candidates up front, one lane each,
     // doubled the registers of the 32-lane kernel and halved its occupancy:
     // generation went from 2.28 s to 2.83 s at n = 1M.)
