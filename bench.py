@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
                     help="timed steps (default 20; 2 for the batched workload, whose step builds 4,096 graphs)")
-    ap.add_argument("--warmup", type=int, default=None, help="warm-up steps (default 3; 1 for the batched workload)")
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--queries", type=int, default=10_000_000)
@@ -65,8 +65,6 @@ def parse():
     heavy = args.workload == "batched"
     if args.steps is None:
         args.steps = 2 if heavy else 20
-    if args.warmup is None:
-        args.warmup = 1 if heavy else 3
     return args
 
 
