@@ -14,9 +14,10 @@
 // change from run to run.  This restatement is deterministic:
 //   1. size[c] = vertices labelled c (exact histogram);
 //   2. every vertex gathers its neighbours' labels, sorts them (warp bitonic
-//      network for rows up to 32, block network in shared memory beyond) and
-//      proposes the most frequent label c with c == own label or
-//      size[c] < G_max, ties to the smaller label (no neighbours: keep);
+//      network, rows up to 32) or counts them in a hash table (a block per
+//      longer row), and proposes the most frequent label c with c == own
+//      label or size[c] < G_max, ties to the smaller label (no neighbours:
+//      keep);
 //   3. join[c] = vertices proposing c != own label; a label's joiners move
 //      iff size[c] + join[c] <= G_max (all or none), so no group exceeds G_max;
 //   4. stop when nothing moves or after max_iterations.
@@ -74,40 +75,6 @@ __global__ void k_lp_sort_small(int32_t n, const int64_t* __restrict__ rp, uint3
   }
 }
 
-// Rows longer than 32 (listed in rows[0..*count)): one block per row, bitonic
-// network in shared memory (cap entries) or in a global scratch row.
-__global__ void k_lp_sort_large(const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
-                                const int64_t* __restrict__ rp, uint32_t* __restrict__ prop, int cap,
-                                uint32_t* __restrict__ gscratch, int64_t gcap) {
-  extern __shared__ uint32_t sm_keys[];
-  const int cnt = *count;
-  for (int r = blockIdx.x; r < cnt; r += gridDim.x) {
-    const int v = rows[r];
-    const int64_t lo = rp[v], len = rp[v + 1] - lo;
-    int64_t P = 1;
-    while (P < len) P <<= 1;
-    uint32_t* a = P <= cap ? sm_keys : gscratch + (int64_t)blockIdx.x * gcap;
-    for (int64_t i = threadIdx.x; i < P; i += blockDim.x) a[i] = i < len ? prop[lo + i] : 0xFFFFFFFFu;
-    for (int64_t size = 2; size <= P; size <<= 1) {
-      for (int64_t stride = size >> 1; stride > 0; stride >>= 1) {
-        __syncthreads();
-        for (int64_t i = threadIdx.x; i < P / 2; i += blockDim.x) {
-          int64_t x = 2 * i - (i & (stride - 1)), y = x + stride;
-          bool up = ((x & size) == 0);
-          uint32_t p = a[x], q = a[y];
-          if ((p > q) == up) {
-            a[x] = q;
-            a[y] = p;
-          }
-        }
-      }
-    }
-    __syncthreads();
-    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) prop[lo + i] = a[i];
-    __syncthreads();
-  }
-}
-
 __global__ void k_lp_list_rows(int32_t n, const int64_t* __restrict__ rp, int32_t* __restrict__ rows,
                                int32_t* __restrict__ count) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
@@ -115,7 +82,7 @@ __global__ void k_lp_list_rows(int32_t n, const int64_t* __restrict__ rp, int32_
 }
 
 // Mode of the sorted neighbour labels among eligible labels (Get_New_Label):
-// one thread per vertex of degree <= 32 (longer rows: k_lp_choose_large).
+// one thread per vertex of degree <= 32 (longer rows: k_lp_mode_large).
 __global__ void k_lp_choose(int32_t n, const int64_t* __restrict__ rp, const uint32_t* __restrict__ prop,
                             const int32_t* __restrict__ label, const int32_t* __restrict__ size, int32_t gmax,
                             int32_t* __restrict__ proposed, int32_t* __restrict__ join) {
@@ -145,48 +112,79 @@ __global__ void k_lp_choose(int32_t n, const int64_t* __restrict__ rp, const uin
   }
 }
 
-// The same for the rows longer than 32 (listed in rows[0..*count)), one warp
-// per row: a lane at the end of a run gets the run's length from the previous
-// run end (a ballot within the chunk, carried across chunks); the warp keeps
-// the eligible run of largest count, the smallest label on ties - the first
-// such run in the sorted row, as the serial scan picks.
-__global__ void k_lp_choose_large(const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
-                                  const int64_t* __restrict__ rp, const uint32_t* __restrict__ prop,
-                                  const int32_t* __restrict__ label, const int32_t* __restrict__ size, int32_t gmax,
-                                  int32_t* __restrict__ proposed, int32_t* __restrict__ join) {
-  const int lane = lane_id();
-  const int64_t nrows = *count;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = warp; r < nrows; r += nwarps) {
+// The same choice for the rows longer than 32 (listed in rows[0..*count)),
+// one block per row, without sorting: the block counts the row's labels in a
+// hash table (shared memory; a per-block table in global scratch for rows of
+// more than kLpModeSlots / 2 entries) and takes the eligible label of largest
+// count, the smaller label on ties - the run the serial scan of the sorted
+// row keeps.  (Sorting the long rows with a block-wide bitonic network and
+// scanning the runs with one warp per row took 93 + 25 ms of the 100 rounds
+// at n = 1M, the network's barriers and the warps on the longest rows setting
+// the time.)
+constexpr int kLpModeSlots = 4096;  // shared-memory table: 32 KB of keys and counts
+
+__global__ void __launch_bounds__(kLpThreads) k_lp_mode_large(
+    const int32_t* __restrict__ rows, const int32_t* __restrict__ count, const int64_t* __restrict__ rp,
+    const uint32_t* __restrict__ prop, const int32_t* __restrict__ label, const int32_t* __restrict__ size,
+    int32_t gmax, int32_t* __restrict__ proposed, int32_t* __restrict__ join, uint32_t* __restrict__ gscratch,
+    int64_t gslots) {
+  __shared__ uint32_t s_key[kLpModeSlots];
+  __shared__ uint32_t s_cnt[kLpModeSlots];
+  __shared__ unsigned long long s_best[kLpThreads / 32];
+  const int nrows = *count;
+  const int lane = lane_id(), wid = threadIdx.x >> 5;
+  for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
     const int v = rows[r];
-    const int32_t own = label[v];
-    const int64_t lo = rp[v], hi = rp[v + 1];
-    unsigned long long best = 0;  // (count << 32) | (0xFFFFFFFF - label); 0 = none
-    int64_t prev_end = lo - 1;
-    for (int64_t base = lo; base < hi; base += 32) {
-      const int64_t i = base + lane;
-      const bool valid = i < hi;
-      const uint32_t c = valid ? prop[i] : 0u;
-      const bool is_end = valid && (i + 1 == hi || prop[i + 1] != c);
-      const unsigned ends = __ballot_sync(0xffffffffu, is_end);
-      if (is_end && ((int32_t)c == own || size[c] < gmax)) {
-        const unsigned below = ends & ((1u << lane) - 1u);
-        const int64_t pe = below ? base + (31 - __clz(below)) : prev_end;
-        const unsigned long long key = ((unsigned long long)(i - pe) << 32) | (0xFFFFFFFFu - c);
-        best = key > best ? key : best;
+    const int64_t lo = rp[v], len = rp[v + 1] - lo;
+    int64_t cap = 64;
+    while (cap < 2 * len) cap <<= 1;
+    uint32_t* key = s_key;
+    uint32_t* cnt = s_cnt;
+    if (cap > kLpModeSlots) {
+      key = gscratch + (int64_t)blockIdx.x * 2 * gslots;
+      cnt = key + gslots;
+    }
+    const uint32_t mask = (uint32_t)cap - 1;
+    for (int64_t i = threadIdx.x; i < cap; i += blockDim.x) {
+      key[i] = 0xFFFFFFFFu;  // no label is all-ones (labels are vertex ids)
+      cnt[i] = 0;
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < len; e += blockDim.x) {
+      const uint32_t c = prop[lo + e];
+      uint32_t ix = table_hash(c, mask);
+      for (uint32_t probe = 0; probe <= mask; probe++) {  // the table is at most half full
+        const uint32_t old = atomicCAS(&key[ix], 0xFFFFFFFFu, c);
+        if (old == 0xFFFFFFFFu || old == c) {
+          atomicAdd(&cnt[ix], 1u);
+          break;
+        }
+        ix = (ix + 1) & mask;
       }
-      if (ends) prev_end = base + (31 - __clz(ends));
+    }
+    __syncthreads();
+    const int32_t own = label[v];
+    unsigned long long best = 0;  // (count << 32) | (0xFFFFFFFF - label); 0 = none
+    for (int64_t i = threadIdx.x; i < cap; i += blockDim.x) {
+      const uint32_t c = key[i];
+      if (c != 0xFFFFFFFFu && ((int32_t)c == own || size[c] < gmax)) {
+        const unsigned long long k = ((unsigned long long)cnt[i] << 32) | (0xFFFFFFFFu - c);
+        best = k > best ? k : best;
+      }
     }
     for (int o = 16; o > 0; o >>= 1) {
       const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
       best = x > best ? x : best;
     }
-    if (lane == 0) {
+    if (lane == 0) s_best[wid] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); w++) best = s_best[w] > best ? s_best[w] : best;
       const int32_t b = best ? (int32_t)(0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFull)) : own;
       proposed[v] = b;
       if (b != own) atomicAdd(&join[b], 1);
     }
+    __syncthreads();  // the next row reuses the table
   }
 }
 
@@ -347,13 +345,11 @@ int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_
   HSDL_TRY(changed.alloc(1, st));
   int64_t maxdeg = 0;
   for (int32_t v = 0; v < n; v++) maxdeg = std::max(maxdeg, g->h_rp[v + 1] - g->h_rp[v]);
-  const int cap = 16384;  // 64 KB of shared memory per block
-  int64_t P = 1;
-  while (P < maxdeg) P <<= 1;
-  const int large_grid = sms * 2;
-  if (P > cap) HSDL_TRY(gscratch.alloc((int64_t)large_grid * P, st));
-  HSDL_CUDA(cudaFuncSetAttribute(k_lp_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(cap * sizeof(uint32_t))));
+  // rows past the shared-memory table count in a per-block global table
+  int64_t gslots = 64;
+  while (gslots < 2 * maxdeg) gslots <<= 1;
+  const int mode_grid = sms * resident_blocks(k_lp_mode_large, kLpThreads);
+  if (gslots > kLpModeSlots) HSDL_TRY(gscratch.alloc((int64_t)mode_grid * 2 * gslots, st));
   const int grid = sms * resident_blocks(k_lp_choose, kLpThreads);
   HSDL_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t), st));
   k_lp_list_rows<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, rows.p, count.p);
@@ -372,15 +368,14 @@ int group_lp(hsdl_graph_impl* g, int32_t gmax, int32_t max_iter, int32_t* group_
       HSDL_LAUNCHED();
       k_lp_sort_small<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, prop.p);
       HSDL_LAUNCHED();
-      k_lp_sort_large<<<large_grid, 512, cap * sizeof(uint32_t), st>>>(rows.p, count.p, g->rp.p, prop.p, cap,
-                                                                       gscratch.p, P);
-      HSDL_LAUNCHED();
     }
     k_lp_choose<<<grid, kLpThreads, 0, st>>>(n, g->rp.p, prop.p, label.p, size.p, gmax, proposed.p, join.p);
     HSDL_LAUNCHED();
-    k_lp_choose_large<<<grid, kLpThreads, 0, st>>>(rows.p, count.p, g->rp.p, prop.p, label.p, size.p, gmax,
-                                                   proposed.p, join.p);
-    HSDL_LAUNCHED();
+    if (m2 > 0) {
+      k_lp_mode_large<<<mode_grid, kLpThreads, 0, st>>>(rows.p, count.p, g->rp.p, prop.p, label.p, size.p, gmax,
+                                                        proposed.p, join.p, gscratch.p, gslots);
+      HSDL_LAUNCHED();
+    }
     k_lp_apply<<<grid, kLpThreads, 0, st>>>(n, label.p, proposed.p, size.p, join.p, gmax, nlabel.p, changed.p);
     HSDL_LAUNCHED();
     std::swap(label.p, nlabel.p);

@@ -11,7 +11,9 @@ def _graphs():
     return [H.HostGraph.chung_lu(8000, 8, 2.2, 800, 1, 100, seed=81),
             H.HostGraph.erdos_renyi(3000, 9000, 1, 100, seed=82),
             H.HostGraph.barabasi_albert(5000, 3, 1, 100, seed=83),
-            H.HostGraph.from_edges(50, [0, 1, 2, 10], [1, 2, 3, 11], [1, 1, 1, 1])]
+            H.HostGraph.from_edges(50, [0, 1, 2, 10], [1, 2, 3, 11], [1, 1, 1, 1]),
+            # rows of several thousand neighbours: past the shared-memory table of the long-row kernel
+            H.HostGraph.chung_lu(20000, 8, 2.1, 5000, 1, 100, seed=84)]
 
 
 @pytest.mark.parametrize("gmax", [1, 7, 64, 1024])
