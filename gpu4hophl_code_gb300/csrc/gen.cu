@@ -560,10 +560,9 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
             if (jp + 1 >= len) k1 = ~0ull;
           }
         };
-        auto probe = [&](uint64_t k, uint32_t fw) {
+        // the table probe of a label whose hub passed the slot's filter
+        auto probe = [&](uint64_t k) {
           const int32_t w = (int32_t)lkey_hub(k);
-          const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
-          if (!((fw >> (fb & 31)) & 1u)) return;
           const int h1 = (int)lkey_hop(k);
           uint32_t ix = table_hash((uint32_t)w, mask);
           for (int pr = 0; pr < cap; pr++) {
@@ -586,7 +585,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         // added to the rows only when the index is finalised.
         if (SELF && v < s_hub && gl == 0) {
           const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)v);
-          probe(lkey((uint32_t)v, 0, 0), __ldg(Fl + (fb >> 5)));
+          if ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u) probe(lkey((uint32_t)v, 0, 0));
         }
         // a step covers 2 P G labels: lane gl takes the pairs at 2 gl + 2 G p
         uint64_t a[2 * P];
@@ -596,16 +595,17 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
           uint64_t b[2 * P];
 #pragma unroll
           for (int p = 0; p < P; p++) load_pair(j0 + 2 * G * P + 2 * gl + 2 * G * p, b[2 * p], b[2 * p + 1]);
+          // the filter bit of each label's hub (0 for labels past the hop bound)
           uint32_t f[2 * P];
 #pragma unroll
           for (int x = 0; x < 2 * P; x++) {
             const uint32_t fb = filter_bit<kSlotFilterBits>(lkey_hub(a[x]));
-            f[x] = (int)lkey_hop(a[x]) <= h ? __ldg(Fl + (fb >> 5)) : 0u;
+            f[x] = (int)lkey_hop(a[x]) <= h ? (__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u : 0u;
           }
           bool past = false;  // a label from a wave after the hub's last hub: the rest of the row is too
 #pragma unroll
           for (int x = 0; x < 2 * P; x++) {
-            if ((int)lkey_hop(a[x]) <= h) probe(a[x], f[x]);
+            if (f[x]) probe(a[x]);
             past |= lkey_hub(a[x]) >= theta;
           }
           scanned += (unsigned long long)min(2 * G * P, len - j0);
