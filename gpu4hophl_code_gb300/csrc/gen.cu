@@ -436,16 +436,6 @@ __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
   ctr->hop_c[h + 1] = c < (unsigned long long)capC ? c : (unsigned long long)capC;
 }
 
-// ---------------------------------------------------------------------------
-// hop round: pruning query (a group of G lanes per candidate)
-// ---------------------------------------------------------------------------
-// A candidate (slot, v) at distance d is kept iff no committed label (w, h1, d1)
-// of v with h1 <= h meets the wave hub's table entry T[w][h - h1] (the least
-// distance from the hub to w within h - h1 hops) at d1 + T <= d: the
-// reference's pruning query (generation.h:146-161).  The G lanes of a group
-// read G labels of v at a time and stop as soon as one dominates.  Warps take
-// 8 candidates per group at a time from a per-hop counter, so candidates with
-// long label lists do not hold back a statically assigned share.
 // Moves a warp's staged kept candidates (slot, v, d, parent) to the wave's
 // found-label lists, and those below their hub's hop bound to the next
 // frontier: one atomic per list per 32 entries.  Every lane calls it.
@@ -478,6 +468,16 @@ __device__ inline void prune_flush(int4* kbuf, int& kn, SlotMap map, int32_t h, 
   kn = 0;
 }
 
+// ---------------------------------------------------------------------------
+// hop round: pruning query (a group of G lanes per candidate)
+// ---------------------------------------------------------------------------
+// A candidate (slot, v) at distance d is kept iff no committed label (w, h1, d1)
+// of v with h1 <= h meets the wave hub's table entry T[w][h - h1] (the least
+// distance from the hub to w within h - h1 hops) at d1 + T <= d: the
+// reference's pruning query (generation.h:146-161).  The G lanes of a group
+// read G labels of v at a time and stop as soon as one dominates.  Groups take
+// kPruneTake candidates at a time from a per-hop counter, so candidates with
+// long label lists do not hold back a statically assigned share.
 // Candidates a lane group takes at a time from the hop's counter: 2 / 4 / 8 /
 // 32 gave generation 1.95 / 1.92 / 1.93 / 2.05 s at n = 1M (larger takes
 // leave a longer tail, smaller ones contend on the counter).
