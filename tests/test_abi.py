@@ -137,3 +137,40 @@ def test_label_record_layout_matches_reference():
 
     assert C.sizeof(hsdl_label) == 16
     assert [f for f, _ in hsdl_label._fields_] == ["hub_vertex", "parent_vertex", "hop", "distance"]
+
+
+def test_python_struct_mirrors_match_the_header(tmp_path):
+    """Every ctypes mirror of a public struct has the header's size and field
+    offsets (a C program compiled against include/hsdl.h prints them)."""
+    import shutil
+    import subprocess
+
+    from gpu4hophl_code_gb300 import _native as N
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = [getattr(N, name) for name in dir(N)
+               if name.startswith("hsdl_") and isinstance(getattr(N, name), type)
+               and issubclass(getattr(N, name), C.Structure)]
+    assert len(structs) >= 8
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "hsdl.h"', "int main(void) {"]
+    for cls in structs:
+        t = cls.__name__
+        lines.append(f'  printf("{t} sizeof %zu\\n", sizeof({t}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{t} {f} %zu\\n", offsetof({t}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c11", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    c_layout = {(a, b): int(c) for a, b, c in (line.split() for line in out if line)}
+    for cls in structs:
+        t = cls.__name__
+        assert c_layout[(t, "sizeof")] == C.sizeof(cls), t
+        for f, _ in cls._fields_:
+            assert c_layout[(t, f)] == getattr(cls, f).offset, (t, f)
