@@ -151,3 +151,20 @@ def test_www_batched_and_case_info(orc):
     assert ci.label_size_before_canonical_repair > ci.label_size_after_canonical_repair
     for v in (0, 7, g.n - 1):
         assert np.array_equal(ci.L[v][:, [0, 2, 3]], canon.row(v)[:, [0, 2, 3]])
+
+
+@pytest.mark.parametrize("case", ["path_k1", "two_components", "single_vertex", "unit_ties_k6"])
+def test_www_edge_cases(orc, case):
+    if case == "path_k1":
+        g, K = H.HostGraph.from_edges(6, [0, 1, 2, 3, 4], [1, 2, 3, 4, 5], [3, 1, 4, 1, 5], rank_by_degree=True), 1
+    elif case == "two_components":
+        g, K = H.HostGraph.from_edges(10, [0, 1, 2, 5, 6], [1, 2, 3, 6, 7], [3, 1, 4, 1, 5], rank_by_degree=True), 3
+    elif case == "single_vertex":
+        g, K = H.HostGraph.from_edges(1, [], [], [], rank_by_degree=False), 2
+    else:
+        g, K = H.HostGraph.erdos_renyi(120, 360, 1, 1, seed=44), 6
+    idx = H.Index.build(H.Graph(g), K, generation=1)
+    off, lab = idx.export()
+    canon = orc.build(g, K, threads=1)
+    assert np.array_equal(off, canon.off)
+    assert np.array_equal(lab[:, [0, 2, 3]], canon.lab[:, [0, 2, 3]])

@@ -75,3 +75,30 @@ def test_oracle_www_matches_compiled_reference(orc):
         r = ref.build(g, K, threads=1, clean=True, www=True)
         o = orc.build(g, K, threads=1, clean=True, www=True)
         assert np.array_equal(r.off, o.off) and np.array_equal(r.lab, o.lab)
+
+
+@pytest.mark.parametrize("case", ["path_k1", "two_components", "single_vertex", "unit_ties_k6", "star_k2"])
+def test_www_edge_cases(orc, case):
+    """Small and degenerate graphs: the 2023WWW search cleans to the HSDL
+    labels, and (where the reference is compiled here) equals the reference
+    before and after the clean."""
+    if case == "path_k1":
+        g, K = H.HostGraph.from_edges(6, [0, 1, 2, 3, 4], [1, 2, 3, 4, 5], [3, 1, 4, 1, 5], rank_by_degree=True), 1
+    elif case == "two_components":
+        g, K = H.HostGraph.from_edges(10, [0, 1, 2, 5, 6], [1, 2, 3, 6, 7], [3, 1, 4, 1, 5], rank_by_degree=True), 3
+    elif case == "single_vertex":
+        g, K = H.HostGraph.from_edges(1, [], [], [], rank_by_degree=False), 2
+    elif case == "unit_ties_k6":
+        g, K = H.HostGraph.erdos_renyi(120, 360, 1, 1, seed=44), 6
+    else:
+        g, K = H.HostGraph.from_edges(9, [0] * 8, list(range(1, 9)), [2, 7, 1, 8, 2, 8, 1, 8]), 2
+    hsdl = orc.build(g, K, threads=1)
+    www = orc.build(g, K, threads=1, www=True)
+    assert np.array_equal(www.off, hsdl.off)
+    assert np.array_equal(www.lab[:, [0, 2, 3]], hsdl.lab[:, [0, 2, 3]])
+    if Reference.available:
+        ref = Reference()
+        for clean in (False, True):
+            r = ref.build(g, K, threads=1, clean=clean, www=True)
+            o = orc.build(g, K, threads=1, clean=clean, www=True)
+            assert np.array_equal(r.off, o.off) and np.array_equal(r.lab, o.lab)
