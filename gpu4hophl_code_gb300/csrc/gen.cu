@@ -348,11 +348,11 @@ __device__ inline void expand_relax(const ExpandTile<TPB>& t, SlotMap map, int32
 // it (the 2023WWW search, generation.h:338-347) every neighbour is.  A tile
 // with more than kExpandHeavy relaxations is not relaxed here: its chunks of
 // kExpandChunk relaxations go to the chunk map for k_expand_heavy, which
-// spreads them over all blocks.  (A block relaxing a whole heavy tile set
-// the launch's time alone: the first hop's frontier is the wave's hubs, 256
-// consecutive ranks of similar degree per tile, so a wave of 4,375 hubs kept
-// 17 blocks busy, and an ncu capture of one expansion showed one SM active
-// for 1.49 M cycles against 13 K on average.)
+// spreads them over all blocks, so that no single block carries a tile's
+// whole work while the others idle (the first hop's frontier is the wave's
+// hubs, 256 consecutive ranks of similar degree per tile: a wave of 4,375
+// hubs is only 17 tiles; an ncu capture of one expansion at n = 200k had one
+// SM active for 1.49 M cycles against 13 K on average).
 template <int TPB>
 __global__ void __launch_bounds__(TPB) k_expand(SlotMap map, int32_t h, int32_t K, int32_t rank_prune, int32_t tiles,
                                                 const int64_t* __restrict__ rp, const int2* __restrict__ adj,
