@@ -11,7 +11,8 @@
 //    a dense row cand[slot][0..n) of packed candidate keys
 //    (distance:32 | hop:4 | parent:28).  A wave runs K hop rounds:
 //      expand: every frontier entry (slot, x, d_x) relaxes the neighbours of x
-//              ranked below the hub; atomicMin on the candidate key keeps the
+//              ranked below the hub (all of them in the 2023WWW search,
+//              generation.h:226-370); atomicMin on the candidate key keeps the
 //              best (distance, hop, parent); the first improvement of a
 //              (slot, v) in this hop appends it to the candidate list.
 //              A candidate that does not beat the best distance of any earlier
