@@ -56,6 +56,11 @@ def parse():
                     help="offered Poisson rates (q/s) for the serving loop; 0 = as fast as the ring allows")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-repeats", type=int, default=3,
+                    help="passes per serving / plain-path sweep step (the worst is reported)")
+    ap.add_argument("--plain-windows", default="0,50,200,500",
+                    help="batching windows (us) of the plain path under Poisson arrivals")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-path sweep")
     ap.add_argument("--workload", choices=["plain", "batched", "stress", "serving-mix"], default="plain",
                     help="batched: many small graphs built together; stress: the 4M-vertex graph with Zipf "
                          "queries; serving-mix: 65 resident graphs, Poisson queries over all of them while new "
@@ -125,6 +130,76 @@ def make_queries(n, nq, K, seed):
     return s, t, k
 
 
+# seeds of the parity sample of the 1M-vertex workload (tests/golden/chung_lu_1m_k5.npz)
+PARITY_QUERY_SEED = 0x50415249
+PARITY_BF_SEED = 0x4246
+
+
+def label_digests(off: np.ndarray, lab: np.ndarray, block: int = 1000) -> dict:
+    """Digests of a label set in the reference's order: sha256 of the offsets
+    (int64[n+1]), sha256 of the (hub, hop, distance) triples (int32[total, 3],
+    the parent is left out: the reference picks it by its heap's tie order), and
+    per block of `block` vertices a 64-bit digest of the block's row lengths
+    and triples.  Hashed block by block, so no 3-column copy of the whole set
+    is made."""
+    import hashlib
+
+    off = np.ascontiguousarray(off, np.int64)
+    n = len(off) - 1
+    hhd = hashlib.sha256()
+    blocks = np.zeros((n + block - 1) // block, np.uint64)
+    for i, a in enumerate(range(0, n, block)):
+        b = min(n, a + block)
+        tri = np.ascontiguousarray(lab[off[a]:off[b]][:, [0, 2, 3]], np.int32).tobytes()
+        hhd.update(tri)
+        hb = hashlib.blake2b(digest_size=8)
+        hb.update(np.diff(off[a:b + 1]).tobytes())
+        hb.update(tri)
+        blocks[i] = np.frombuffer(hb.digest(), np.uint64)[0]
+    return {"off": hashlib.sha256(off.tobytes()).hexdigest(), "hhd": hhd.hexdigest(), "blocks": blocks}
+
+
+HEADLINE_FIXTURE = os.path.join(ROOT, "tests", "golden", "headline", "chung_lu_1m_k5.npz")
+
+
+def headline_parity(g, off, lab, query) -> dict | None:
+    """Checks a built 1M-vertex index against the reference's own output on
+    the same workload (tests/golden/headline/chung_lu_1m_k5.npz, made by
+    tests/golden/make_golden_1m.py from CPU_HopHL compiled in place): the
+    label digests, the reference's answers on 100,000 seeded queries and the
+    reference's hop-bounded Bellman-Ford distances on 20,000 sampled pairs.
+    `query(s, t, k)` answers through the GPU path.  None if the fixture is
+    absent or was made for another graph."""
+    if not os.path.exists(HEADLINE_FIXTURE):
+        return None
+    z = np.load(HEADLINE_FIXTURE)
+    if int(z["n"]) != g.n or str(z["graph_digest"]) != graph_digest(g):
+        return None
+    d = label_digests(off, lab)
+    blocks_bad = int(np.count_nonzero(d["blocks"] != z["block_digests"])) if len(d["blocks"]) == len(
+        z["block_digests"]) else -1
+    got = query(z["q_s"], z["q_t"], z["q_k"])
+    bf = query(z["bf_s"], z["bf_t"], z["bf_k"])
+    return {"labels_digest_match": d["hhd"] == str(z["hhd_digest"]) and d["off"] == str(z["off_digest"]),
+            "labels": int(len(lab)), "reference_labels": int(z["n_labels"]),
+            "vertex_blocks_differing": blocks_bad,
+            "reference_answers_checked": int(len(got)),
+            "reference_answer_mismatches": int(np.count_nonzero(got != z["q_ans"])),
+            "bf_pairs": int(len(bf)), "bf_mismatches": int(np.count_nonzero(bf != z["bf_dist"])),
+            "source": "CPU_HopHL (reference, compiled in place, "
+                      f"{int(z['ref_threads'])} threads) labels digest, answers and Bellman-Ford distances"}
+
+
+def graph_digest(g) -> str:
+    """sha256 of the ranked CSR (row offsets, neighbours, weights)."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in (g.row_ptr, g.col, g.w):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
 def algorithmic_bytes(off: np.ndarray, s, t, k, per_label: int = 12) -> int:
     """Per query: per_label bytes for every label of both rows (the join must
     read every one) and 32 B for the two offset pairs - the per-query figure
@@ -138,23 +213,45 @@ def algorithmic_bytes(off: np.ndarray, s, t, k, per_label: int = 12) -> int:
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_query_traffic_chung_lu_1m_10Mq.md")
+QUERY_KERNEL_SOURCES = [os.path.join(ROOT, "gpu4hophl_code_gb300", "csrc", f) for f in ("query.cu", "query_join.cuh")]
 
 
-def captured_traffic(args):
+def query_kernel_digest() -> str:
+    """sha256 (first 16 hex digits) of the query kernel's source files; a
+    traffic capture records it, so a capture of older code is seen as stale."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in QUERY_KERNEL_SOURCES:
+        h.update(open(f, "rb").read())
+    return h.hexdigest()[:16]
+
+
+def captured_traffic(args) -> dict | None:
     """DRAM bytes (read + write) of one k_query launch of this workload, as
-    captured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass)
-    and recorded in the profile summary's line 'traffic per launch: <bytes>'.
-    Only the default workload (n = 1M, 10M queries) was captured; None for
-    any other."""
+    captured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) and
+    recorded in the profile summary's lines 'traffic per launch: <bytes>' and
+    'kernel source sha256: <digest>'.  Returns {"bytes", "capture",
+    "kernel_source_sha256", "current"}; "current" is false when the query
+    kernel's source has changed since the capture (the figure is then not
+    used).  Only the default workload (n = 1M, 10M queries, K = 5) is
+    described; None for any other."""
     if args.n != 1_000_000 or args.queries != 10_000_000 or args.K != 5:
         return None
+    rec = {"bytes": None, "capture": os.path.relpath(TRAFFIC_PROFILE, ROOT), "kernel_source_sha256": None}
     try:
         for line in open(TRAFFIC_PROFILE):
-            if line.lower().startswith("traffic per launch:"):
-                return int(line.split(":", 1)[1].strip().split()[0].replace(",", ""))
+            low = line.lower()
+            if low.startswith("traffic per launch:"):
+                rec["bytes"] = int(line.split(":", 1)[1].strip().split()[0].replace(",", ""))
+            elif low.startswith("kernel source sha256:"):
+                rec["kernel_source_sha256"] = line.split(":", 1)[1].strip().split()[0]
     except OSError:
-        pass
-    return None
+        return None
+    if rec["bytes"] is None:
+        return None
+    rec["current"] = rec["kernel_source_sha256"] == query_kernel_digest()
+    return rec
 
 
 def build_algorithmic_bytes(info: dict) -> int:
@@ -228,6 +325,81 @@ def whole_job_rate(dist, world: int, units_per_rank: float, seconds: float) -> t
     is all ranks' units over the slowest rank's time.  Returns (rate, t_max)."""
     t_max = max_over_ranks(dist, seconds)
     return world * units_per_rank / t_max, t_max
+
+
+def _summary(r) -> dict:
+    return {"qps": r["achieved_qps"], "p50_us": r["p50_us"], "p99_us": r["p99_us"], "p999_us": r["p999_us"],
+            "max_us": r["max_us"]}
+
+
+def _worst(passes: list[dict]) -> dict:
+    """A sweep step over repeated passes: the lowest rate and the highest
+    latency percentiles seen."""
+    w = {"qps": min(p["qps"] for p in passes)}
+    for key in ("p50_us", "p99_us", "p999_us", "max_us"):
+        w[key] = max(p[key] for p in passes)
+    return {k: round(v, 1) for k, v in w.items()}
+
+
+def _best_under(runs: list[dict], p99_us: float = 1000.0) -> dict | None:
+    ok = [x for x in runs if x["p99_us"] < p99_us]
+    return max(ok, key=lambda x: x["qps"]) if ok else None
+
+
+def sweep_serving(H, idx, s, t, k, answers, rates, args, dist) -> dict:
+    """The serving loop (hsdl_serve_*) at each offered Poisson rate, repeated
+    args.serve_repeats times with different arrival seeds; every answer is
+    compared with the batched path's."""
+    srv = H.Server()
+    gid = srv.add_index(idx)
+    runs = []
+    for rate in rates:
+        nreq = args.queries if rate <= 0 else int(min(args.queries, max(100000, rate * args.serve_seconds)))
+        passes = []
+        for rep in range(args.serve_repeats):
+            barrier(dist)
+            r = srv.loadgen(np.full(nreq, gid, np.int32), s[:nreq], t[:nreq], k[:nreq], offered_qps=rate,
+                            seed=1 + rep)
+            assert np.array_equal(r["answers"], answers[:nreq]), "serving answers differ from the batched path"
+            passes.append(_summary(r))
+        runs.append({"offered_qps": rate, "requests": nreq, "passes": len(passes), **_worst(passes)})
+    srv.close()
+    best = _best_under(runs)
+    top = best or max(runs, key=lambda x: x["qps"])
+    return {"qps": top["qps"], "p50_us": top["p50_us"], "p99_us": top["p99_us"], "p999_us": top["p999_us"],
+            "offered_qps": top["offered_qps"], "p99_under_1ms": best is not None, "runs": runs}
+
+
+def sweep_plain(idx, hs, ht, hk, answers, rates, args, dist) -> dict:
+    """The plain path under the serving sweep's arrival streams: hsdl_query_batch
+    on pinned host arrays, one call at a time, each call taking every request
+    that has arrived once the oldest waiting one has waited `window` us
+    (hsdl_query_loadgen).  For each window the rates run upwards until the path
+    saturates (achieved < 0.9 x offered, or p99 over 5 ms)."""
+    import torch
+
+    out = torch.empty(len(answers), dtype=torch.int32).pin_memory()
+    runs = []
+    for window in [float(x) for x in args.plain_windows.split(",")]:
+        for rate in sorted(r for r in rates if r > 0):
+            nreq = int(min(args.queries, max(100000, rate * args.serve_seconds)))
+            passes = []
+            for rep in range(args.serve_repeats):
+                barrier(dist)
+                r = idx.loadgen(hs[:nreq], ht[:nreq], hk[:nreq], offered_qps=rate, window_us=window, seed=1 + rep,
+                                answers=out.numpy()[:nreq])
+                assert np.array_equal(out.numpy()[:nreq], answers[:nreq]), "plain-path answers differ"
+                passes.append({**_summary(r), "mean_batch": r["mean_batch"]})
+            step = {"window_us": window, "offered_qps": rate, "requests": nreq, "passes": len(passes),
+                    **_worst(passes), "mean_batch": round(min(p["mean_batch"] for p in passes), 1)}
+            runs.append(step)
+            if step["qps"] < 0.9 * rate or step["p99_us"] > 5000.0:
+                break
+    best = _best_under(runs)
+    return {"qps": best["qps"] if best else None, "p50_us": best["p50_us"] if best else None,
+            "p99_us": best["p99_us"] if best else None, "offered_qps": best["offered_qps"] if best else None,
+            "window_us": best["window_us"] if best else None, "path": "hsdl_query_batch, pinned host arrays",
+            "runs": runs}
 
 
 def run_ours(args, dist, rank, world, local):
@@ -311,26 +483,15 @@ def run_ours(args, dist, rank, world, local):
     e2e_batch, e2e_s = whole_job_rate(dist, world, args.queries * args.steps, time.perf_counter() - t0)
     assert np.array_equal(ho.numpy(), answers), "e2e answers differ from the device-path answers"
 
-    # persistent serving loop: open-loop Poisson arrivals from host memory
-    serving = None
+    # the persistent serving loop, and the plain path (hsdl_query_batch) under
+    # the same open-loop Poisson streams (same seeds), every sweep step
+    # repeated and reported by its worst pass
+    serving = plain = None
     if not args.no_serve:
-        srv = H.Server()
-        gid = srv.add_index(idx)
-        runs = []
-        for rate in [float(x) for x in args.serve_rates.split(",")]:
-            nreq = args.queries if rate <= 0 else int(min(args.queries, max(100000, rate * args.serve_seconds)))
-            barrier(dist)
-            r = srv.loadgen(np.full(nreq, gid, np.int32), s[:nreq], t[:nreq], k[:nreq], offered_qps=rate)
-            assert np.array_equal(r["answers"], answers[:nreq]), "serving answers differ from the batched path"
-            runs.append({"offered_qps": rate, "requests": nreq, "qps": round(r["achieved_qps"], 1),
-                         "p50_us": round(r["p50_us"], 1), "p99_us": round(r["p99_us"], 1),
-                         "p999_us": round(r["p999_us"], 1), "max_us": round(r["max_us"], 1)})
-        srv.close()
-        ok = [x for x in runs if x["p99_us"] < 1000.0]
-        best = max(ok, key=lambda x: x["qps"]) if ok else max(runs, key=lambda x: x["qps"])
-        serving = {"qps": best["qps"], "p50_us": best["p50_us"], "p99_us": best["p99_us"],
-                   "p999_us": best["p999_us"], "offered_qps": best["offered_qps"],
-                   "p99_under_1ms": bool(ok), "runs": runs}
+        rates = [float(x) for x in args.serve_rates.split(",")]
+        serving = sweep_serving(H, idx, s, t, k, answers, rates, args, dist)
+        if not args.no_plain:
+            plain = sweep_plain(idx, hs.numpy(), ht.numpy(), hk.numpy(), answers, rates, args, dist)
     clk = clocks.stop()
 
     # roofline of the query kernel
@@ -344,13 +505,16 @@ def run_ours(args, dist, rank, world, local):
     res = {}
     if rank == 0:
         off, lab = idx.export()
+        # parity against the reference's own output on this workload (untimed)
+        parity = headline_parity(g, off, lab, idx.query) if args.K == 5 else None
         bytes_per_launch = algorithmic_bytes(off, s, t, k)
+        cap = captured_traffic(args)
         launch_s = kernel_ms / 1000.0 / args.steps
         achieved = bytes_per_launch / launch_s / 1e9
         packed = algorithmic_bytes(off, s, t, k, per_label=8)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
-                "traffic": captured_traffic(args),
+                "traffic": (cap["bytes"] if cap and cap["current"] else None), "traffic_capture": cap,
                 "kernel": "k_query", "algorithmic_bytes_per_launch": bytes_per_launch,
                 "bytes_per_query": round(bytes_per_launch / args.queries, 1),
                 "byte_model": "12 B per label of both rows + 32 B of row offsets per query",
@@ -385,6 +549,12 @@ def run_ours(args, dist, rank, world, local):
             "e2e_batch": {"value": round(e2e_batch, 1), "unit": "queries/s", "path": "hsdl_query_batch, pinned buffers",
                           "h2d_bytes_per_step": 12 * args.queries, "d2h_bytes_per_step": 4 * args.queries},
             "serving": serving,
+            "plain_path": plain,
+            "serving_vs_plain": ({"ratio": round(serving["qps"] / plain["qps"], 3), "target": 10.0,
+                                  "met": serving["qps"] >= 10.0 * plain["qps"] and serving["p99_under_1ms"],
+                                  "rule": "best q/s whose worst-pass p99 < 1 ms, serving loop over plain path"}
+                                 if serving and plain and plain["qps"] else None),
+            "parity": parity,
             "build": {"seconds": round(build_s, 3),
                       "seconds_with_grouping_and_csr": round(build_s + lp_s + graph_dev_s, 3),
                       "generate_s": round(info["time_generate_s"], 3),

@@ -69,7 +69,13 @@ class hsdl_loadgen_result(C.Structure):
     _fields_ = [("completed", C.c_int64), ("seconds", C.c_double), ("achieved_qps", C.c_double),
                 ("offered_qps", C.c_double), ("p50_us", C.c_double), ("p90_us", C.c_double),
                 ("p99_us", C.c_double), ("p999_us", C.c_double), ("max_us", C.c_double),
-                ("ready_frac", C.c_double)]
+                ("ready_frac", C.c_double), ("mean_batch", C.c_double)]
+
+
+class hsdl_query_loadgen_opts(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("reserved", C.c_int32), ("n", C.c_int64), ("s", C.c_void_p),
+                ("t", C.c_void_p), ("k", C.c_void_p), ("answers", C.c_void_p), ("offered_qps", C.c_double),
+                ("seed", C.c_uint64), ("window_us", C.c_double)]
 
 
 class hsdl_serve_counters(C.Structure):
@@ -93,6 +99,7 @@ SIGNATURES = {
     "hsdl_last_error": (C.c_char_p, []),
     "hsdl_version": (I32, []),
     "hsdl_launch_count": (I64, []),
+    "hsdl_debug_inject_failure": (C.c_int, [I32, I32]),
     "hsdl_gen_erdos_renyi": (C.c_int, [I32, I64, I32, I32, C.c_uint64, PP]),
     "hsdl_gen_chung_lu": (C.c_int, [I32, C.c_double, C.c_double, C.c_double, I32, I32, C.c_uint64, PP]),
     "hsdl_gen_barabasi_albert": (C.c_int, [I32, I32, I32, I32, C.c_uint64, PP]),
@@ -118,6 +125,7 @@ SIGNATURES = {
     "hsdl_query_batch": (C.c_int, [P, I64, P, P, P, P]),
     "hsdl_query_batch_device": (C.c_int, [P, I64, P, P, P, P, P]),
     "hsdl_query_batch_static": (C.c_int, [P, I64, P, P, P, P]),
+    "hsdl_query_static_prepare": (C.c_int, []),
     "hsdl_extract_path": (C.c_int, [P, I32, I32, I32, P, I32, C.POINTER(I32)]),
     "hsdl_index_get_info": (C.c_int, [P, C.POINTER(hsdl_index_info)]),
     "hsdl_export": (C.c_int, [P, P, P]),
@@ -137,6 +145,7 @@ SIGNATURES = {
     "hsdl_serve_submit": (C.c_int, [P, I64, P, P, P, P, C.POINTER(I64)]),
     "hsdl_serve_wait": (C.c_int, [P, I64, I64, P, C.c_double]),
     "hsdl_serve_loadgen": (C.c_int, [P, C.POINTER(hsdl_loadgen_opts), C.POINTER(hsdl_loadgen_result)]),
+    "hsdl_query_loadgen": (C.c_int, [P, C.POINTER(hsdl_query_loadgen_opts), C.POINTER(hsdl_loadgen_result)]),
     "hsdl_serve_stats": (C.c_int, [P, C.POINTER(hsdl_serve_counters)]),
     "hsdl_serve_destroy": (C.c_int, [P]),
 }

@@ -22,6 +22,23 @@ thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 
+std::atomic<int32_t>* failure_budget() {
+  static std::atomic<int32_t> budget[HSDL_FAIL_SITE_MAX + 1];
+  return budget;
+}
+
+bool injected_failure(int site) {
+  std::atomic<int32_t>& b = failure_budget()[site];
+  int32_t c = b.load();
+  while (c > 0) {
+    if (b.compare_exchange_weak(c, c - 1)) {
+      set_error("injected failure at site " + std::to_string(site));
+      return true;
+    }
+  }
+  return false;
+}
+
 std::atomic<int64_t>& launch_counter() {
   static std::atomic<int64_t> c{0};
   return c;
@@ -105,13 +122,27 @@ int fetch_row(hsdl_index* idx, int32_t v, std::vector<uint64_t>& k, std::vector<
   return HSDL_OK;
 }
 
+// Largest label set an import accepts (2^36 labels = 1 TiB of 16-byte records).
+constexpr int64_t kMaxImportLabels = int64_t(1) << 36;
+
 int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label* labels, hsdl_index* idx) {
   HSDL_CHECK_ARG(n >= 1 && n <= (int32_t)kIdMask, "vertex count out of range");
   HSDL_CHECK_ARG(K >= 1 && K <= kMaxK, "K must be in [1, 14]");
   HSDL_CHECK_ARG(offsets && offsets[0] == 0, "offsets[0] must be 0");
   int64_t total = offsets[n];
-  std::vector<uint64_t> keys((size_t)total);
-  std::vector<int32_t> par((size_t)total);
+  // bounds before any host allocation: a corrupt count must come back as an
+  // error, not as an exception through the C ABI
+  HSDL_CHECK_ARG(total >= 0 && total <= kMaxImportLabels, "label count out of range");
+  HSDL_CHECK_ARG(total == 0 || labels, "null label array");
+  std::vector<uint64_t> keys;
+  std::vector<int32_t> par;
+  try {
+    keys.resize((size_t)total);
+    par.resize((size_t)total);
+  } catch (const std::exception&) {
+    set_error("host memory for " + std::to_string(total) + " labels");
+    return HSDL_ERR_NOMEM;
+  }
   int64_t mr = 0;
   for (int32_t v = 0; v < n; v++) {
     HSDL_CHECK_ARG(offsets[v + 1] >= offsets[v], "offsets must be non-decreasing");
@@ -196,6 +227,12 @@ const char* hsdl_last_error(void) { return last_error_cstr(); }
 int32_t hsdl_version(void) { return 1; }
 int64_t hsdl_launch_count(void) { return launch_counter().load(); }
 
+int hsdl_debug_inject_failure(int32_t site, int32_t count) {
+  HSDL_CHECK_ARG(site >= 1 && site <= HSDL_FAIL_SITE_MAX && count >= 0, "unknown failure site or negative count");
+  failure_budget()[site].store(count);
+  return HSDL_OK;
+}
+
 // ---------------------------------------------------------------------------
 // host graphs
 // ---------------------------------------------------------------------------
@@ -272,13 +309,22 @@ int hsdl_read_graph_text(const char* path, int32_t rank_by_degree, hsdl_host_gra
     std::string tag;
     if (!(ss >> tag)) continue;
     if (tag == "|V|=") {
-      ss >> n;
+      if (!(ss >> n) || n < 1 || n > (int64_t)kIdMask) {
+        set_error("|V|= out of range [1, 2^28): " + line);
+        return HSDL_ERR_INVALID;
+      }
     } else if (tag == "Edge") {
       long long x, y;
       double wt;
       if (!(ss >> x >> y >> wt)) {
         set_error("malformed Edge line: " + line);
         return HSDL_ERR_IO;
+      }
+      // range-checked before the narrowing casts, so an oversized id cannot
+      // wrap into a valid one
+      if (x < 0 || y < 0 || x > INT32_MAX || y > INT32_MAX || !(wt >= INT32_MIN && wt <= INT32_MAX)) {
+        set_error("Edge line out of the int32 range: " + line);
+        return HSDL_ERR_INVALID;
       }
       a.push_back((int32_t)x);
       b.push_back((int32_t)y);
@@ -659,18 +705,33 @@ int hsdl_load_labels(const char* path, int32_t K, hsdl_index** out) {
     set_error(std::string("cannot open ") + path);
     return HSDL_ERR_IO;
   }
+  // every count is checked against the bytes left in the file before it
+  // sizes anything, so a corrupt count is an error, not a huge allocation
+  std::fseek(f, 0, SEEK_END);
+  const long long file_bytes = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
   size_t V = 0;
-  bool ok = std::fread(&V, sizeof(size_t), 1, f) == 1 && V >= 1 && V <= kIdMask;
-  std::vector<int64_t> off(ok ? V + 1 : 1, 0);
+  bool ok = file_bytes > 0 && std::fread(&V, sizeof(size_t), 1, f) == 1 && V >= 1 && V <= kIdMask &&
+            (long long)(V * sizeof(size_t)) <= file_bytes;
+  std::vector<int64_t> off;
   std::vector<hsdl_label> lab;
-  for (size_t v = 0; ok && v < V; v++) {
-    size_t c = 0;
-    ok = std::fread(&c, sizeof(size_t), 1, f) == 1 && c <= ((size_t)1 << 40);
-    if (!ok) break;
-    size_t at = lab.size();
-    lab.resize(at + c);
-    if (c) ok = std::fread(lab.data() + at, sizeof(hsdl_label), c, f) == c;
-    off[v + 1] = (int64_t)lab.size();
+  try {
+    off.assign(ok ? V + 1 : 1, 0);
+    for (size_t v = 0; ok && v < V; v++) {
+      size_t c = 0;
+      ok = std::fread(&c, sizeof(size_t), 1, f) == 1;
+      const long long left = file_bytes - std::ftell(f);
+      ok = ok && c <= (size_t)std::max(0LL, left) / sizeof(hsdl_label);
+      if (!ok) break;
+      size_t at = lab.size();
+      lab.resize(at + c);
+      if (c) ok = std::fread(lab.data() + at, sizeof(hsdl_label), c, f) == c;
+      off[v + 1] = (int64_t)lab.size();
+    }
+  } catch (const std::exception&) {
+    std::fclose(f);
+    set_error(std::string("host memory while reading ") + path);
+    return HSDL_ERR_NOMEM;
   }
   std::fclose(f);
   if (!ok) {

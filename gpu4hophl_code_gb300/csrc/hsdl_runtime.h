@@ -164,6 +164,12 @@ int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32
 // smallest index of a query with s or t outside [0, n), all-ones if none.
 int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, unsigned long long* d_first,
                     cudaStream_t st);
+// Loads every variant of the query kernel and the id check on the current
+// device (cudaFuncGetAttributes forces a lazily loaded kernel to load).
+int preload_query_kernels();
+// Host-side failure injection for tests (hsdl_debug_inject_failure): true if
+// the pass through `site` must fail; the error text is set.
+bool injected_failure(int site);
 int sort_rows(int32_t n, const int64_t* d_off, uint64_t* key, int32_t* par, int64_t max_row, cudaStream_t st);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st);  // out[n] = total
 

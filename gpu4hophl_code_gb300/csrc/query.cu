@@ -86,6 +86,18 @@ int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const in
   return HSDL_OK;
 }
 
+int preload_query_kernels() {
+  cudaFuncAttributes a;
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<8, false>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<8, true>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<16, false>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<16, true>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<32, false>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<32, true>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_first_bad_id));
+  return HSDL_OK;
+}
+
 int query_device(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                  int32_t* out, cudaStream_t st) {
   if (nq <= 0) return HSDL_OK;

@@ -215,6 +215,46 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
 double mono_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+// Scheduled arrival times (ns from the run's start) of n requests of a
+// Poisson stream of rate qps (SplitMix64 uniforms, exponential gaps); all at
+// 0 for qps <= 0.
+std::vector<int64_t> poisson_arrivals_ns(int64_t n, double qps, uint64_t seed) {
+  std::vector<int64_t> arrive((size_t)n);
+  uint64_t z = seed ? seed : 0x9E3779B97F4A7C15ull;
+  double tcur = 0;
+  for (int64_t i = 0; i < n; i++) {
+    if (qps > 0) {
+      z += 0x9E3779B97F4A7C15ull;
+      uint64_t x = z;
+      x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+      x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+      x ^= x >> 31;
+      double u = ((double)(x >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+      tcur += -std::log(u) / qps;
+    }
+    arrive[i] = (int64_t)(tcur * 1e9);
+  }
+  return arrive;
+}
+
+// Rate and latency percentiles of a load run (latencies in ns).
+void summarise_latency(const std::vector<int32_t>& lat_ns, int64_t first_arrival, int64_t last_done, double offered,
+                       hsdl_loadgen_result* res) {
+  std::vector<int32_t> sorted(lat_ns);
+  std::sort(sorted.begin(), sorted.end());
+  auto pct = [&](double p) { return sorted[std::min<size_t>(sorted.size() - 1, (size_t)(p * (sorted.size() - 1)))]; };
+  const int64_t n = (int64_t)lat_ns.size();
+  res->completed = n;
+  res->seconds = (double)(last_done - first_arrival) / 1e9;
+  res->achieved_qps = res->seconds > 0 ? (double)n / res->seconds : 0;
+  res->offered_qps = offered;
+  res->p50_us = pct(0.50) / 1e3;
+  res->p90_us = pct(0.90) / 1e3;
+  res->p99_us = pct(0.99) / 1e3;
+  res->p999_us = pct(0.999) / 1e3;
+  res->max_us = sorted.back() / 1e3;
+}
+
 int64_t mono_ns() {
   return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
       .count();
@@ -683,23 +723,7 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
   std::lock_guard<std::mutex> lk(S->mu);
   const uint64_t base = S->tail;
   SRV_ARG(S->consumed == S->tail, "loadgen needs every earlier answer to be read first");
-  std::vector<int64_t> arrive((size_t)n);
-  {
-    uint64_t z = o->seed ? o->seed : 0x9E3779B97F4A7C15ull;
-    double tcur = 0;
-    for (int64_t i = 0; i < n; i++) {
-      if (o->offered_qps > 0) {
-        z += 0x9E3779B97F4A7C15ull;
-        uint64_t x = z;
-        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-        x ^= x >> 31;
-        double u = ((double)(x >> 11) + 0.5) * (1.0 / 9007199254740992.0);
-        tcur += -std::log(u) / o->offered_qps;
-      }
-      arrive[i] = (int64_t)(tcur * 1e9);
-    }
-  }
+  std::vector<int64_t> arrive = poisson_arrivals_ns(n, o->offered_qps, o->seed);
   std::vector<int32_t> lat_ns((size_t)n);
   // Answers arrive in host memory over the host link; reading them one line
   // (8 answers) at a time from a single thread serialises a link round trip
@@ -806,19 +830,43 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
     set_error("serving loop stopped answering during the load run");
     return HSDL_ERR_TIMEOUT;
   }
-  std::vector<int32_t> sorted(lat_ns);
-  std::sort(sorted.begin(), sorted.end());
-  auto pct = [&](double p) { return sorted[std::min<size_t>(sorted.size() - 1, (size_t)(p * (sorted.size() - 1)))]; };
-  res->completed = n;
-  res->seconds = (double)(last_done - arrive[0]) / 1e9;
-  res->achieved_qps = res->seconds > 0 ? (double)n / res->seconds : 0;
-  res->offered_qps = o->offered_qps;
-  res->p50_us = pct(0.50) / 1e3;
-  res->p90_us = pct(0.90) / 1e3;
-  res->p99_us = pct(0.99) / 1e3;
-  res->p999_us = pct(0.999) / 1e3;
-  res->max_us = sorted.back() / 1e3;
+  summarise_latency(lat_ns, arrive[0], last_done, o->offered_qps, res);
   res->ready_frac = (double)ready_first.load() / (double)n;
+  res->mean_batch = 0;
+  return HSDL_OK;
+}
+
+// The plain path under the same open-loop Poisson stream: requests that have
+// arrived are answered in batches by hsdl_query_batch (host arrays in, host
+// arrays out, one call at a time).  A batch is dispatched once the oldest
+// waiting request has waited window_us and the previous call has returned,
+// and takes every request that has arrived by then.  Latency runs from a
+// request's scheduled arrival to the return of the call that answered it.
+int hsdl_query_loadgen(hsdl_index* idx, const hsdl_query_loadgen_opts* o, hsdl_loadgen_result* res) {
+  SRV_ARG(idx && o && res, "null argument");
+  SRV_ARG(o->struct_size == (int32_t)sizeof(hsdl_query_loadgen_opts), "hsdl_query_loadgen_opts.struct_size mismatch");
+  const int64_t n = o->n;
+  SRV_ARG(n >= 1 && o->s && o->t && o->k && o->answers && o->window_us >= 0, "bad request arrays");
+  std::vector<int64_t> arrive = poisson_arrivals_ns(n, o->offered_qps, o->seed);
+  std::vector<int32_t> lat_ns((size_t)n);
+  const int64_t window_ns = (int64_t)(o->window_us * 1e3);
+  const int64_t t_start = mono_ns() + 1000000;
+  int64_t done = 0, batches = 0;
+  for (int64_t i = 0; i < n;) {
+    const int64_t dispatch = std::max(done, arrive[i] + window_ns);
+    int64_t now;
+    while ((now = mono_ns() - t_start) < dispatch) {
+    }
+    int64_t j = std::upper_bound(arrive.begin() + i, arrive.end(), now) - arrive.begin();
+    HSDL_TRY(hsdl_query_batch(idx, j - i, o->s + i, o->t + i, o->k + i, o->answers + i));
+    done = mono_ns() - t_start;
+    for (int64_t r = i; r < j; r++) lat_ns[r] = (int32_t)std::min<int64_t>(INT32_MAX, done - arrive[r]);
+    batches++;
+    i = j;
+  }
+  summarise_latency(lat_ns, arrive[0], done, o->offered_qps, res);
+  res->ready_frac = 0;
+  res->mean_batch = (double)n / (double)batches;
   return HSDL_OK;
 }
 

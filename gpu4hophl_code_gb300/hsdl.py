@@ -338,6 +338,28 @@ class Index:
         check(lib().hsdl_query_batch_device(self._h, nq, C.c_void_p(d_s), C.c_void_p(d_t), C.c_void_p(d_k),
                                             C.c_void_p(d_out), C.c_void_p(stream) if stream else None))
 
+    def loadgen(self, s, t, k, offered_qps: float, window_us: float = 0.0, seed: int = 1, answers=None) -> dict:
+        """The plain path (hsdl_query_batch) under an open-loop Poisson stream
+        of rate offered_qps, batched by arrival window (hsdl_query_loadgen).
+        Pass pinned host arrays (e.g. torch pin_memory().numpy()) for a fair
+        rate; `answers` (int32, len(s)) receives the answers."""
+        s = np.ascontiguousarray(s, np.int32)
+        t = np.ascontiguousarray(t, np.int32)
+        k = np.ascontiguousarray(k, np.int32)
+        ans = np.zeros(len(s), np.int32) if answers is None else answers
+        o = N.hsdl_query_loadgen_opts()
+        o.struct_size = C.sizeof(N.hsdl_query_loadgen_opts)
+        o.n = len(s)
+        o.s, o.t, o.k, o.answers = s.ctypes.data, t.ctypes.data, k.ctypes.data, ans.ctypes.data
+        o.offered_qps = offered_qps
+        o.seed = seed
+        o.window_us = window_us
+        r = N.hsdl_loadgen_result()
+        check(lib().hsdl_query_loadgen(self._h, C.byref(o), C.byref(r)))
+        res = {f: getattr(r, f) for f, _ in N.hsdl_loadgen_result._fields_}
+        res["answers"] = ans
+        return res
+
     def path(self, s: int, t: int, k: int, cap: int = 64):
         e = np.zeros((cap, 2), np.int32)
         cnt = C.c_int32()

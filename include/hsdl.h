@@ -49,6 +49,15 @@ const char* hsdl_last_error(void);
 int32_t hsdl_version(void);
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t hsdl_launch_count(void);
+/* Host-side failure injection, for tests of error paths (no counterpart in
+ * the reference): the next `count` passes through failure site `site` return
+ * HSDL_ERR_CUDA with the message "injected failure at site <site>", without
+ * touching the GPU.  Sites: HSDL_FAIL_STATIC_QUERY = inside
+ * hsdl_query_batch_static, after its input copies and id check are queued
+ * and before the query kernel.  count = 0 disarms. */
+#define HSDL_FAIL_STATIC_QUERY 1
+#define HSDL_FAIL_SITE_MAX 1
+int hsdl_debug_inject_failure(int32_t site, int32_t count);
 
 /* ------------------------------------------------------------------------
  * Host graphs: seeded synthetic generators and loaders.  The result is an
@@ -211,16 +220,24 @@ int hsdl_query_batch_device(hsdl_index* idx, int64_t nq, const int32_t* d_s, con
  * answers are staged in one fixed-size device array inside the library
  * instead of per-call allocations.  For callers that cannot allocate device
  * memory - next to running serving or build kernels (cudaMalloc/cudaFree can
- * synchronise the device), under another allocator's hard cap, or while a
- * CUDA graph is captured in global mode.  This entry point has no counterpart
- * in the reference.  At most HSDL_STATIC_QUERY_MAX queries per call (larger
- * batches: HSDL_ERR_INVALID).  The array (16 MiB) is held by every GPU that
- * loads the library until exit; the first call on a device looks up its
- * address, so make it before any stream capture.  Calls share the array and
- * are serialised by a process-wide lock (overlapping calls would race). */
+ * synchronise the device), or under another allocator's hard cap.  This entry
+ * point has no counterpart in the reference.  At most HSDL_STATIC_QUERY_MAX
+ * queries per call (larger batches: HSDL_ERR_INVALID); a batch naming a vertex
+ * outside the index is HSDL_ERR_INVALID after the call, as in
+ * hsdl_query_batch.  The array (16 MiB) is placed on a device when the
+ * library's module is loaded there - at the set-up, since modules load lazily
+ * - and held until exit.  Set-up, once per device with the device current:
+ * hsdl_query_static_prepare, or else the first hsdl_query_batch_static call;
+ * it looks up the array's address and loads every query kernel variant, and a
+ * module load may synchronise the device, so run it before a serving loop
+ * starts or any stream capture begins.  Calls share the array and are
+ * serialised by a process-wide lock that is held until the call's work on the
+ * stream has finished, on error paths too (overlapping calls would race). */
 #define HSDL_STATIC_QUERY_MAX (1 << 20)
 int hsdl_query_batch_static(hsdl_index* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k,
                             int32_t* out);
+/* The set-up of hsdl_query_batch_static on the current device (idempotent). */
+int hsdl_query_static_prepare(void);
 
 /* Launch parameters of the query kernel for one index (the autotuner's
  * knobs): threads per block (multiple of 32, 32..1024), how many queries
@@ -330,7 +347,22 @@ typedef struct hsdl_loadgen_result {
   double offered_qps;
   double p50_us, p90_us, p99_us, p999_us, max_us; /* arrival -> answer seen */
   double ready_frac;   /* answers already present when the host first looked */
+  double mean_batch;   /* hsdl_query_loadgen: mean requests per hsdl_query_batch call */
 } hsdl_loadgen_result;
+
+/* The plain path under the same Poisson stream (hsdl_query_loadgen). */
+typedef struct hsdl_query_loadgen_opts {
+  int32_t struct_size; /* sizeof(hsdl_query_loadgen_opts) */
+  int32_t reserved;
+  int64_t n;           /* requests (all on the one index) */
+  const int32_t* s;    /* source, target, hop bound per request (pinned host memory for a fair rate) */
+  const int32_t* t;
+  const int32_t* k;
+  int32_t* answers;    /* answers, in request order */
+  double offered_qps;  /* Poisson arrival rate (the serving loadgen's stream for the same seed) */
+  uint64_t seed;
+  double window_us;    /* a batch leaves once its oldest request has waited this long and the GPU is free */
+} hsdl_query_loadgen_opts;
 
 typedef struct hsdl_serve_counters {
   int64_t submitted, processed, bad_requests;
@@ -356,6 +388,12 @@ int hsdl_serve_submit(hsdl_server* srv, int64_t n, const int32_t* g, const int32
 /* Reads the answers of the oldest unread tickets [first_ticket, +n). */
 int hsdl_serve_wait(hsdl_server* srv, int64_t first_ticket, int64_t n, int32_t* answers, double timeout_s);
 int hsdl_serve_loadgen(hsdl_server* srv, const hsdl_loadgen_opts* opts, hsdl_loadgen_result* result);
+/* Open-loop load on the plain path: the same Poisson arrivals answered in
+ * batches by hsdl_query_batch, one call at a time; latency from scheduled
+ * arrival to the return of the answering call.  No counterpart in the
+ * reference (its gpu_query answers one query per three launches,
+ * Query_mdnd/src/gpu_query.cu:139-155). */
+int hsdl_query_loadgen(hsdl_index* idx, const hsdl_query_loadgen_opts* opts, hsdl_loadgen_result* result);
 int hsdl_serve_stats(hsdl_server* srv, hsdl_serve_counters* stats);
 int hsdl_serve_destroy(hsdl_server* srv);
 

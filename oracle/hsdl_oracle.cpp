@@ -785,6 +785,8 @@ struct OrcGroup {
 
 extern "C" {
 
+int orc_lp_assemble(int n, const int64_t* rp, const int32_t* label, int gmax, int32_t* group_of_vertex);
+
 // Deterministic capped label propagation + the reference's group assembly.
 //  Propagation (GPU_Community_Detection.cuh:29-91, made deterministic):
 //   size[c] = |{v : label v = c}|; every vertex takes the most frequent label
@@ -839,6 +841,12 @@ int orc_lp_group(int n, const int64_t* rp, const int32_t* col, int gmax, int max
     }
   }
   if (iterations) *iterations = it;
+  return orc_lp_assemble(n, rp, label.data(), gmax, group_of_vertex);
+}
+
+// The reference's group assembly alone (CDLP_group.cuh:39-100) on given
+// propagation labels (each in [0, n)).
+int orc_lp_assemble(int n, const int64_t* rp, const int32_t* label, int gmax, int32_t* group_of_vertex) {
   std::vector<std::vector<int32_t>> buckets(n), groups;
   for (int v = 0; v < n; v++) buckets[label[v]].push_back(v);
   for (auto& b : buckets)

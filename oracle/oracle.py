@@ -22,20 +22,42 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libhsdl_ref.so")
-REF_DIR_DEFAULT = "/root/reference"
+REF_LP_LIB = os.path.join(HERE, "_ref", "libcdlp_ref.so")
+
+
+def reference_dir() -> str:
+    """The reference checkout the checkers read: $HSDL_REFERENCE_DIR, else the
+    location oracle/Makefile names (it may not exist on this machine)."""
+    d = os.environ.get("HSDL_REFERENCE_DIR") or os.environ.get("HSDL_REF_DIR")
+    if d:
+        return d
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref-dir"], capture_output=True, text=True)
+    return r.stdout.strip()
 
 
 def build(ref_dir: str | None = None) -> None:
-    """Compiles liboracle.so, and _ref/libhsdl_ref.so when the reference
-    checkout exists."""
+    """Compiles liboracle.so, and _ref/libhsdl_ref.so when a reference
+    checkout exists: `ref_dir`, else $HSDL_REFERENCE_DIR, else the location
+    oracle/Makefile names."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    ref_dir = ref_dir or os.environ.get("HSDL_REFERENCE_DIR", REF_DIR_DEFAULT)
-    if os.path.isdir(os.path.join(ref_dir, "CPU_HopHL", "include")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True)
+    ref_dir = ref_dir or os.environ.get("HSDL_REFERENCE_DIR")
+    subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"] + ([f"REF_DIR={ref_dir}"] if ref_dir else []),
+                   check=True)
 
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class CsrGraph:
+    """A ranked CSR graph (n, row_ptr int64[n+1], col int32[2m], w int32[2m])."""
+
+    def __init__(self, n: int, row_ptr: np.ndarray, col: np.ndarray, w: np.ndarray):
+        self.n, self.row_ptr, self.col, self.w = int(n), row_ptr, col, w
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.row_ptr[-1]) // 2
 
 
 class Labels:
@@ -77,7 +99,26 @@ class Oracle:
         L.orc_bf.argtypes = [i32, vp, vp, vp, i32, i32, vp]
         L.orc_lp_group.restype = i32
         L.orc_lp_group.argtypes = [i32, vp, vp, i32, i32, vp, vp]
+        L.orc_lp_assemble.restype = i32
+        L.orc_lp_assemble.argtypes = [i32, vp, vp, i32, vp]
+        L.orc_gen_chung_lu.restype = vp
+        L.orc_gen_chung_lu.argtypes = [i32, C.c_double, C.c_double, C.c_double, i32, i32, C.c_uint64, vp]
+        L.orc_graph_copy.argtypes = [vp, vp, vp, vp]
+        L.orc_graph_free.argtypes = [vp]
         self.L = L
+
+    def chung_lu(self, n: int, avg_degree: float, exponent: float, max_degree: float, wmin: int, wmax: int,
+                 seed: int) -> "CsrGraph":
+        """The seeded Chung-Lu workload graph, ranked (the generator the
+        product library uses, compiled into this library)."""
+        m2 = np.zeros(1, np.int64)
+        h = self.L.orc_gen_chung_lu(n, avg_degree, exponent, max_degree, wmin, wmax, seed, _p(m2))
+        try:
+            g = CsrGraph(n, np.zeros(n + 1, np.int64), np.zeros(int(m2[0]), np.int32), np.zeros(int(m2[0]), np.int32))
+            self.L.orc_graph_copy(h, _p(g.row_ptr), _p(g.col), _p(g.w))
+        finally:
+            self.L.orc_graph_free(h)
+        return g
 
     # -- handles -------------------------------------------------------------
     def _export(self, h) -> Labels:
@@ -147,6 +188,14 @@ class Oracle:
         ng = self.L.orc_lp_group(g.n, _p(g.row_ptr), _p(g.col), max_group, max_iterations, _p(gov), _p(it))
         return gov, int(ng), int(it[0])
 
+    def lp_assemble(self, g, labels, max_group: int):
+        """The group assembly alone on given propagation labels (each in
+        [0, n)); returns (group_of_vertex, number of groups)."""
+        lab = np.ascontiguousarray(labels, np.int32)
+        gov = np.zeros(g.n, np.int32)
+        ng = self.L.orc_lp_assemble(g.n, _p(g.row_ptr), _p(lab), max_group, _p(gov))
+        return gov, int(ng)
+
 
 class Reference:
     """The reference's own CPU_HopHL (compiled from its headers in place)."""
@@ -195,6 +244,26 @@ class Reference:
         e = np.zeros((cap, 2), np.int32)
         c = self.L.ref_path(s, t, k, _p(e), cap)
         return [tuple(x) for x in e[:max(c, 0)].tolist()]
+
+
+class ReferenceLP:
+    """The reference's own LP group assembly (CDLP_group.cuh:39-100) compiled
+    in place, fed given propagation labels (oracle/ref_lp_driver.cpp)."""
+
+    available = os.path.exists(REF_LP_LIB)
+
+    def __init__(self, path: str = REF_LP_LIB):
+        L = C.CDLL(path)
+        vp, i32 = C.c_void_p, C.c_int
+        L.ref_lp_assemble.restype = i32
+        L.ref_lp_assemble.argtypes = [i32, vp, vp, vp, i32, vp]
+        self.L = L
+
+    def assemble(self, g, labels, max_group: int):
+        lab = np.ascontiguousarray(labels, np.int32)
+        gov = np.zeros(g.n, np.int32)
+        ng = self.L.ref_lp_assemble(g.n, _p(g.row_ptr), _p(g.col), _p(lab), max_group, _p(gov))
+        return gov, int(ng)
 
 
 class OracleIndex:

@@ -74,8 +74,42 @@ def make_www(name: str, g, K: int):
     print(f"www/{name}: n={g.n} m={g.num_edges} K={K} labels {len(raw.lab)} -> {len(cln.lab)}")
 
 
+def lp_label_sets(n: int, gmax: int, seed: int) -> np.ndarray:
+    """Propagation labels for the assembly: groups of random sizes up to
+    gmax (half of them single vertices) with random label values in [0, n);
+    values that collide merge groups, so some exceed gmax."""
+    rng = np.random.default_rng(seed)
+    lab = np.empty(n, np.int32)
+    perm = rng.permutation(n)
+    v = 0
+    while v < n:
+        sz = int(min(n - v, rng.integers(1, gmax + 1) if rng.random() < 0.5 else 1))
+        lab[perm[v:v + sz]] = rng.integers(0, n)
+        v += sz
+    return lab
+
+
+def make_lp():
+    """The reference's LP group assembly (CDLP_group.cuh:39-100, compiled in
+    place by oracle/Makefile into _ref/libcdlp_ref.so) on fixed propagation
+    labels: the deterministic half of generate_Group_CDLP."""
+    R = O.ReferenceLP()
+    cases = {}
+    for gseed in (0, 1):
+        g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=gseed)
+        for gmax in (1, 5, 64, 1024):
+            lab = lp_label_sets(g.n, gmax, seed=100 * gseed + gmax)
+            gov, ng = R.assemble(g, lab, gmax)
+            key = f"g{gseed}_m{gmax}"
+            cases[key + "_labels"] = lab
+            cases[key + "_gov"] = gov
+    os.makedirs(os.path.join(OUT, "lp"), exist_ok=True)
+    np.savez_compressed(os.path.join(OUT, "lp", "assembly.npz"), **cases)
+    print(f"lp/assembly: {len(cases) // 2} label sets")
+
+
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else O.REF_DIR_DEFAULT
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
     O.build(ref_dir)
     # the reference's own fixture graphs (ids re-ranked by degree, ties by id)
     for fname, K in (("simple_iterative_tests.txt", 5), ("euroroad2.txt", 5)):
@@ -94,6 +128,7 @@ def main():
     make_www("er_150_600_k4", H.HostGraph.erdos_renyi(150, 600, 1, 100, seed=9), 4)
     make_www("er_300_unit_k3", H.HostGraph.erdos_renyi(300, 900, 1, 1, seed=8), 3)
     make_www("cl_600_k5", H.HostGraph.chung_lu(600, 6, 2.2, 80, 1, 100, seed=10), 5)
+    make_lp()
 
 
 if __name__ == "__main__":

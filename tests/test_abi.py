@@ -90,6 +90,33 @@ def test_from_edges_and_text_reader(built, tmp_path):
     r.validate()
 
 
+@pytest.mark.parametrize("text", ["|V|= 4294967301\nEdge 0 1 5\n", "|V|= 5\nEdge 0 4294967299 5\n",
+                                  "|V|= 5\nEdge -1 2 5\n", "|V|= 5\nEdge 0 1 1e12\n"])
+def test_text_reader_rejects_values_outside_int32(built, tmp_path, text):
+    """Ids, counts and weights are range-checked before they are narrowed to
+    int32, so an oversized value cannot wrap into a valid small one."""
+    from gpu4hophl_code_gb300 import HostGraph, HsdlError
+
+    p = tmp_path / "g.txt"
+    p.write_text(text)
+    with pytest.raises(HsdlError) as e:
+        HostGraph.read_text(str(p))
+    assert e.value.code == 1 and "range" in str(e.value)
+
+
+def test_label_file_with_a_corrupt_count_is_an_error(built, tmp_path):
+    """A row count larger than the rest of the file is reported before any
+    buffer is sized by it (no device is touched on this path)."""
+    from gpu4hophl_code_gb300 import HsdlError, Index
+
+    p = tmp_path / "labels.bin"
+    p.write_bytes(np.array([2, 1], np.uint64).tobytes() + np.array([0, 0, 0, 0], np.int32).tobytes() +
+                  np.array([1 << 39], np.uint64).tobytes())
+    with pytest.raises(HsdlError) as e:
+        Index.load(str(p), 3)
+    assert e.value.code == 7 and "malformed" in str(e.value)
+
+
 @pytest.mark.parametrize("case", ["selfloop", "asym", "unsorted", "weight0", "range"])
 def test_malformed_csr_is_rejected_with_a_message(built, case):
     from gpu4hophl_code_gb300 import HostGraph, HsdlError

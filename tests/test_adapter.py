@@ -17,9 +17,9 @@ LIBDIR = os.path.join(ROOT, "gpu4hophl_code_gb300")
 
 
 def _ref_dir():
-    from oracle.oracle import REF_DIR_DEFAULT
+    from oracle.oracle import reference_dir
 
-    return os.environ.get("HSDL_REF_DIR", REF_DIR_DEFAULT)
+    return reference_dir()
 
 
 def test_adapter_binds_to_the_reference_types():

@@ -32,6 +32,7 @@ def test_build_byte_models():
 def test_captured_traffic_is_read_from_the_committed_profile():
     args = argparse.Namespace(n=1_000_000, queries=10_000_000, K=5)
     v = bench.captured_traffic(args)
-    assert isinstance(v, int) and v > 0
+    assert isinstance(v["bytes"], int) and v["bytes"] > 0
+    assert v["capture"].startswith("profiles/") and isinstance(v["current"], bool)
     args.n = 200_000
     assert bench.captured_traffic(args) is None

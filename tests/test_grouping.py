@@ -1,10 +1,61 @@
 """Label-propagation grouping (generate_Group_CDLP,
 Hybrid_Generation_Clean/include/vgroup/CDLP_group.cuh:20): the oracle's
-deterministic restatement on the CPU, and the GPU kernels against it."""
+deterministic restatement on the CPU, and the GPU kernels against it.
+
+The reference's propagation (CDLP_GPU) caps groups with racy atomics, so only
+its second half - the group assembly (CDLP_group.cuh:39-100: bucketing by
+label, greedy merge of small groups, ordering by total degree) - is
+deterministic and can be pinned: the oracle's assembly is compared with the
+reference's own code on fixed propagation labels, through a committed fixture
+(tests/golden/lp/assembly.npz, made by tests/golden/make_golden.py) and, where
+the reference is compiled here, live."""
+import os
+
 import numpy as np
 import pytest
 
 import gpu4hophl_code_gb300 as H
+from conftest import GOLDEN
+
+LP_FIXTURE = os.path.join(GOLDEN, "lp", "assembly.npz")
+
+
+def _lp_cases():
+    z = np.load(LP_FIXTURE)
+    for gseed in (0, 1):
+        g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=gseed)
+        for gmax in (1, 5, 64, 1024):
+            key = f"g{gseed}_m{gmax}"
+            yield g, gmax, z[key + "_labels"], z[key + "_gov"]
+
+
+def test_assembly_matches_the_reference_fixture(orc):
+    n = 0
+    for g, gmax, lab, want in _lp_cases():
+        gov, ng = orc.lp_assemble(g, lab, gmax)
+        assert ng == int(want.max()) + 1
+        assert np.array_equal(gov, want), (gmax, ng)
+        n += 1
+    assert n == 8
+
+
+def test_assembly_matches_the_reference_live(orc):
+    from oracle.oracle import ReferenceLP
+
+    if not ReferenceLP.available:
+        pytest.skip("the reference's group assembly is not compiled here")
+    R = ReferenceLP()
+    rng = np.random.default_rng(3)
+    for seed in range(4):
+        g = H.HostGraph.barabasi_albert(2000, 3, 1, 100, seed=seed)
+        for gmax in (2, 17, 300):
+            # propagation labels: the oracle's own grouping at another cap,
+            # and random groups
+            lab = orc.lp_group(g, max(1, gmax // 2), 20)[0]
+            for labels in (lab, rng.integers(0, g.n, g.n).astype(np.int32)):
+                a = orc.lp_assemble(g, labels, gmax)
+                b = R.assemble(g, labels, gmax)
+                assert a[1] == b[1] and np.array_equal(a[0], b[0])
 
 
 def _graphs():

@@ -1,11 +1,17 @@
 """hsdl_query_batch_static: the query entry point that allocates no device
-memory (for callers that must not call cudaMalloc - e.g. next to a running
-serving or build kernel, where cudaMalloc/cudaFree can synchronise the device,
-or under another allocator's hard cap).  It stages queries and answers in a
-fixed library-owned device array; this test calls it through the C ABI twice
-in a row and compares with the allocating entry point hsdl_query_batch
-(integer answers: exact).  Collected last so a stop-at-first-failure run has
-already run every other test."""
+memory.  It is for callers that must not call cudaMalloc: a thread answering
+queries next to a running serving loop or build (cudaMalloc/cudaFree can
+synchronise the device and stall those kernels), or a process whose device
+memory is owned by another allocator with a hard cap.  It stages queries and
+answers in a fixed library-owned device array.
+
+These tests call it through the C ABI: twice in a row against the allocating
+entry point hsdl_query_batch (integer answers: exact), after a failure
+injected on the host once work is queued (the lock must not be released while
+that work can still touch the shared array), with ids outside the index, and
+inside another stream's global-mode graph capture on the same thread (where
+CUDA refuses cudaMalloc: the call must still succeed).  Collected last so a
+stop-at-first-failure run has already run every other test."""
 import ctypes as C
 
 import numpy as np
@@ -18,21 +24,38 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def test_static_staging_matches_allocating_query(built):
+@pytest.fixture(scope="module")
+def index(built):
     import gpu4hophl_code_gb300 as H
     from gpu4hophl_code_gb300 import _native
 
-    fn = built.hsdl_query_batch_static
+    # set-up before anything else runs on the device
+    assert built.hsdl_query_static_prepare() == 0, _native.last_error()
     g = H.HostGraph.chung_lu(20000, 8, 2.2, 500, 1, 100, seed=31)
     dev = H.Graph(g)
     idx = H.Index.build(dev, 5)
+    yield g, idx
+    idx.close()
+    dev.close()
+
+
+def _batch(rng, n, nq):
+    s = rng.integers(0, n, nq).astype(np.int32)
+    t = rng.integers(0, n, nq).astype(np.int32)
+    k = rng.integers(-1, 7, nq).astype(np.int32)
+    return s, t, k
+
+
+def test_static_staging_matches_allocating_query(built, index):
+    from gpu4hophl_code_gb300 import _native
+
+    g, idx = index
+    fn = built.hsdl_query_batch_static
     rng = np.random.default_rng(5)
     # two calls in a row; the second is smaller so stale entries of the first
     # would show up if the staging array were read past nq
     for nq in (300_000, 123_457):
-        s = rng.integers(0, g.n, nq).astype(np.int32)
-        t = rng.integers(0, g.n, nq).astype(np.int32)
-        k = rng.integers(-1, 7, nq).astype(np.int32)
+        s, t, k = _batch(rng, g.n, nq)
         got = np.full(nq, -7, np.int32)
         rc = fn(idx.handle, nq, _p(s), _p(t), _p(k), _p(got))
         assert rc == 0, _native.last_error()
@@ -44,5 +67,59 @@ def test_static_staging_matches_allocating_query(built):
     rc = fn(idx.handle, big, _p(one), _p(one), _p(one), _p(one))
     assert rc == _native.HSDL_ERR_INVALID
     assert "HSDL_STATIC_QUERY_MAX" in _native.last_error()
-    idx.close()
-    dev.close()
+
+
+def test_failure_after_queued_work_leaves_the_next_call_correct(built, index):
+    from gpu4hophl_code_gb300 import _native
+
+    g, idx = index
+    fn = built.hsdl_query_batch_static
+    rng = np.random.default_rng(6)
+    s, t, k = _batch(rng, g.n, 1 << 20)
+    out = np.zeros(len(s), np.int32)
+    assert built.hsdl_debug_inject_failure(1, 1) == 0
+    rc = fn(idx.handle, len(s), _p(s), _p(t), _p(k), _p(out))
+    assert rc == _native.HSDL_ERR_CUDA and "injected failure" in _native.last_error()
+    s2, t2, k2 = _batch(rng, g.n, 200_000)
+    got = np.zeros(len(s2), np.int32)
+    assert fn(idx.handle, len(s2), _p(s2), _p(t2), _p(k2), _p(got)) == 0, _native.last_error()
+    assert np.array_equal(got, idx.query(s2, t2, k2))
+
+
+def test_ids_outside_the_index_are_rejected(built, index):
+    from gpu4hophl_code_gb300 import _native
+
+    g, idx = index
+    fn = built.hsdl_query_batch_static
+    s = np.array([0, 1, g.n, 2], np.int32)
+    t = np.array([1, 2, 3, -1], np.int32)
+    k = np.full(4, 3, np.int32)
+    out = np.zeros(4, np.int32)
+    rc = fn(idx.handle, 4, _p(s), _p(t), _p(k), _p(out))
+    assert rc == _native.HSDL_ERR_INVALID and "out of range at query 2" in _native.last_error()
+
+
+def test_call_succeeds_inside_a_global_mode_capture(built, index):
+    """While this thread captures another stream in global mode, CUDA refuses
+    calls that may allocate or synchronise the device; the static entry point
+    makes none.  Nothing is enqueued on the captured stream; the empty graph is
+    discarded."""
+    import torch
+
+    from gpu4hophl_code_gb300 import _native
+
+    g, idx = index
+    fn = built.hsdl_query_batch_static
+    rng = np.random.default_rng(7)
+    s, t, k = _batch(rng, g.n, 50_000)
+    want = idx.query(s, t, k)
+    got = np.zeros(len(s), np.int32)
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    rc = None
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="global"):
+        rc = fn(idx.handle, len(s), _p(s), _p(t), _p(k), _p(got))
+        err = _native.last_error()
+    del graph
+    assert rc == 0, err
+    assert np.array_equal(got, want)
