@@ -586,49 +586,62 @@ def run_ours(args, dist, rank, world, local):
 
 
 def run_reference(args, dist, rank, world, local):
-    """The reference's CPU query path on all host cores over the same labels.
-    The labels are the canonical set (bit-identical to CPU_HopHL's output for
-    this order and K); they are produced once on the GPU as untimed input
-    because the CPU build of a 1M-vertex index takes tens of minutes."""
+    """The reference's CPU path on all host cores, on this workload, without
+    the product library: the oracle's restatement of CPU_HopHL builds the
+    canonical index (hop_constrained_two_hop_labels_generation, generation +
+    sortL + canonical repair with the reference's thread-pool schedule,
+    CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:513-632,
+    its phase timers at :594-629) from the same seeded graph (the workload
+    generator compiled into the oracle library), then answers the same query
+    batches with hop_constrained_extract_distance
+    (CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels.h:144) split over
+    the cores.  Rank 0 only."""
     if rank != 0:
         return None
-    import torch
+    from oracle.oracle import Oracle
 
-    torch.cuda.set_device(local)
-    import gpu4hophl_code_gb300 as H
-
-    g = make_graph(args.n)
-    dev = H.Graph(g)
-    idx = H.Index.build(dev, args.K, clean=True)
-    off, lab = idx.export()
-    idx.close()
-    dev.close()
-    s, t, k = make_queries(args.n, args.queries, args.K, seed=1000)
-    from oracle.oracle import Labels, Oracle
-
-    ix = Oracle().index(Labels(off, lab))  # label conversion is setup, not timed
     threads = os.cpu_count() or 1
-    per_step = max(50000, min(args.queries, 4_000_000))
-    for i in range(max(1, args.warmup)):
-        ix.query(s[:50000], t[:50000], k[:50000], threads=threads)
+    orc = Oracle()
+    g = orc.chung_lu(args.n, 10.0, 2.1, 10000.0, 1, 100, SEED)
     t0 = time.perf_counter()
-    done = 0
+    labels = orc.build(g, args.K, threads=threads)
+    build_s = time.perf_counter() - t0
+    build_phases = {"seconds": round(build_s, 3), "generate_s": round(float(labels.info["t_gen"]), 3),
+                    "sort_s": round(float(labels.info["t_sort"]), 3), "clean_s": round(float(labels.info["t_clean"]), 3),
+                    "labels": int(len(labels.lab)), "labels_before_clean": int(labels.info["before"]),
+                    "threads": threads,
+                    "timers": "time_generate_labels, time_sortL, time_canonical_repair of the reference's driver"}
+    parity = None
+    if args.K == 5 and os.path.exists(HEADLINE_FIXTURE):
+        z = np.load(HEADLINE_FIXTURE)
+        if int(z["n"]) == g.n and str(z["graph_digest"]) == graph_digest(g):
+            d = label_digests(labels.off, labels.lab)
+            parity = {"labels_digest_match": d["hhd"] == str(z["hhd_digest"]) and d["off"] == str(z["off_digest"]),
+                      "labels": int(len(labels.lab)), "reference_labels": int(z["n_labels"])}
+    s, t, k = make_queries(args.n, args.queries, args.K, seed=1000)
+    ix = orc.index(labels)  # label conversion is setup, not timed
+    del labels
+    per_step = args.queries
+    for i in range(max(1, args.warmup)):
+        ix.query(s, t, k, threads=threads)
+    t0 = time.perf_counter()
     for i in range(args.steps):
-        lo = (i * per_step) % max(1, args.queries - per_step + 1)
-        ix.query(s[lo:lo + per_step], t[lo:lo + per_step], k[lo:lo + per_step], threads=threads)
-        done += per_step
+        ix.query(s, t, k, threads=threads)
     secs = time.perf_counter() - t0
     ix.close()
-    v = done / secs
+    v = per_step * args.steps / secs
     return {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "queries/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1000 / args.steps, 3),
+            "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": round(secs * 1000 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded Chung-Lu graph and uniform queries)",
             "config": {"workload": f"chung_lu n={args.n} avg_deg=10 gamma=2.1 max_deg=10000 w=[1,100] K={args.K}; "
-                                   f"uniform (s,t,k) queries, k in [1,{args.K}]",
+                                   f"{args.queries} uniform (s,t,k) queries per step, k in [1,{args.K}]",
                        "n": args.n, "K": args.K, "queries_per_step": per_step, "parallelism": "cpu"},
             "cpu_baseline": {"value": round(v, 1), "unit": "queries/s", "cores": threads, "kind": "port",
-                             "sample": f"{per_step} queries per step over the 1M-vertex canonical labels"},
+                             "sample": f"{args.steps} steps of all {per_step} queries over the CPU-built canonical "
+                                       f"labels of the 1M-vertex graph",
+                             "build_s": round(build_s, 3), "build": build_phases},
+            "build": build_phases, "parity": parity,
             "e2e": {"value": round(v, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -50,7 +50,8 @@ class hsdl_index_info(C.Structure):
                 ("work_join_reads", C.c_int64), ("work_labels_written", C.c_int64), ("work_clean_reads", C.c_int64),
                 ("work_candidates", C.c_int64), ("work_join_visible", C.c_int64),
                 ("build_peak_bytes", C.c_int64), ("build_pool_entries", C.c_int64),
-                ("build_max_candidates", C.c_int64), ("build_wave_splits", C.c_int32), ("build_pool_chunks", C.c_int32)]
+                ("build_max_candidates", C.c_int64), ("build_wave_splits", C.c_int32), ("build_pool_chunks", C.c_int32),
+                ("query_key_bytes", C.c_int32), ("query_key_hub_bits", C.c_int32)]
 
 
 class hsdl_serve_opts(C.Structure):
@@ -100,6 +101,7 @@ SIGNATURES = {
     "hsdl_version": (I32, []),
     "hsdl_launch_count": (I64, []),
     "hsdl_debug_inject_failure": (C.c_int, [I32, I32]),
+    "hsdl_debug_pool_used_high": (C.c_int, [P, I32]),
     "hsdl_gen_erdos_renyi": (C.c_int, [I32, I64, I32, I32, C.c_uint64, PP]),
     "hsdl_gen_chung_lu": (C.c_int, [I32, C.c_double, C.c_double, C.c_double, I32, I32, C.c_uint64, PP]),
     "hsdl_gen_barabasi_albert": (C.c_int, [I32, I32, I32, I32, C.c_uint64, PP]),

@@ -102,6 +102,7 @@ void free_index(hsdl_index* idx) {
   if (idx->stream) cudaStreamSynchronize(idx->stream);
   idx->off.release();
   idx->key.release();
+  idx->key32.release();
   idx->par.release();
   idx->wave_lo.release();
   if (idx->stream) {
@@ -179,7 +180,7 @@ int upload_index(int32_t n, int32_t K, const int64_t* offsets, const hsdl_label*
   }
   HSDL_CUDA(cudaStreamSynchronize(st));
   idx->h_off.assign(offsets, offsets + n + 1);
-  return HSDL_OK;
+  return make_query_keys(idx);
 }
 
 }  // namespace
@@ -226,6 +227,22 @@ extern "C" {
 const char* hsdl_last_error(void) { return last_error_cstr(); }
 int32_t hsdl_version(void) { return 1; }
 int64_t hsdl_launch_count(void) { return launch_counter().load(); }
+
+int hsdl_debug_pool_used_high(int64_t* bytes, int32_t reset) {
+  HSDL_CHECK_ARG(bytes, "null argument");
+  int dev = 0;
+  HSDL_CUDA(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  HSDL_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+  if (reset) {
+    unsigned long long zero = 0;
+    HSDL_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+  }
+  unsigned long long v = 0;
+  HSDL_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &v));
+  *bytes = (int64_t)v;
+  return HSDL_OK;
+}
 
 int hsdl_debug_inject_failure(int32_t site, int32_t count) {
   HSDL_CHECK_ARG(site >= 1 && site <= HSDL_FAIL_SITE_MAX && count >= 0, "unknown failure site or negative count");
@@ -484,6 +501,7 @@ int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index
   HSDL_TRY(new_index(&idx));
   int rc = build_index(g, K, o, idx);
   if (rc == HSDL_OK && o.clean) rc = clean_index(idx);
+  if (rc == HSDL_OK) rc = make_query_keys(idx);
   if (rc != HSDL_OK) {
     free_index(idx);
     return rc;
@@ -495,7 +513,8 @@ int hsdl_build(hsdl_graph* g, int32_t K, const hsdl_build_opts* opts, hsdl_index
 int hsdl_clean(hsdl_index* idx) {
   HSDL_CHECK_ARG(idx, "null index");
   if (idx->cleaned) return HSDL_OK;
-  return clean_index(idx);
+  HSDL_TRY(clean_index(idx));
+  return make_query_keys(idx);
 }
 
 // ---------------------------------------------------------------------------
@@ -619,7 +638,9 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->labels = idx->total;
   info->labels_before_clean = idx->before;
   info->labels_after_clean = idx->after;
-  info->device_bytes = idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
+  info->device_bytes = idx->off.bytes() + idx->key.bytes() + idx->key32.bytes() + idx->par.bytes();
+  info->query_key_bytes = idx->key32.p ? 4 : 8;
+  info->query_key_hub_bits = idx->key32.p ? 32 - (int32_t)idx->fmt32.hub_shift : 0;
   info->time_generate_s = idx->t_gen;
   info->time_sort_s = idx->t_sort;
   info->time_clean_s = idx->t_clean;

@@ -46,6 +46,30 @@ __host__ __device__ inline uint32_t lkey_hd(uint64_t k) { return (uint32_t)k; }
 __host__ __device__ inline uint32_t lkey_hop(uint64_t k) { return hd_hop((uint32_t)k); }
 __host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return hd_dist((uint32_t)k); }
 
+// Compact query key (4 B), used by the query joins when the index's ranges
+// fit: hub:H | hop:P | distance:D with H = bits of n - 1, P = bits of K and
+// D = 32 - H - P >= the bits of the largest distance in the index (n = 1M,
+// K = 5, weights <= 100: 20 | 3 | 9).  Unsigned order is again the label
+// order, so the rows keep their sort; a join streams half the bytes of the
+// 8-byte keys.  Indexes whose ranges do not fit keep only the 8-byte keys.
+struct Fmt64 {
+  __host__ __device__ uint32_t hub(uint64_t k) const { return (uint32_t)(k >> 32); }
+  __host__ __device__ uint32_t hop(uint64_t k) const { return hd_hop((uint32_t)k); }
+  __host__ __device__ uint32_t dist(uint64_t k) const { return hd_dist((uint32_t)k); }
+};
+struct Fmt32 {
+  uint32_t hub_shift;  // P + D
+  uint32_t dist_bits;  // D
+  __host__ __device__ uint32_t hub(uint32_t k) const { return k >> hub_shift; }
+  __host__ __device__ uint32_t hop(uint32_t k) const {
+    return (k >> dist_bits) & ((1u << (hub_shift - dist_bits)) - 1u);
+  }
+  __host__ __device__ uint32_t dist(uint32_t k) const { return k & ((1u << dist_bits) - 1u); }
+  __host__ __device__ uint32_t pack(uint32_t hub, uint32_t hop, uint32_t dist) const {
+    return (hub << hub_shift) | (hop << dist_bits) | dist;
+  }
+};
+
 __host__ __device__ inline uint64_t ckey(uint32_t dist, uint32_t hop, uint32_t parent) {
   return ((uint64_t)dist << 32) | ((uint64_t)hop << 28) | (uint64_t)parent;
 }

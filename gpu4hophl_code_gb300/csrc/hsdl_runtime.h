@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/hsdl.h"
+#include "hsdl_device.cuh"
 
 namespace hsdl {
 
@@ -107,6 +108,8 @@ struct hsdl_index_impl {
   DevBuf<uint64_t> key;   // hub:32 | hop:4 | distance:28
   DevBuf<int32_t> par;    // parent_vertex
   DevBuf<int32_t> wave_lo;    // generated, not yet cleaned: first hub of each hub's wave
+  DevBuf<uint32_t> key32;     // compact query keys (Fmt32), when the index's ranges fit; else empty
+  Fmt32 fmt32{0, 0};
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
@@ -167,6 +170,9 @@ int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const in
 // Loads every variant of the query kernel and the id check on the current
 // device (cudaFuncGetAttributes forces a lazily loaded kernel to load).
 int preload_query_kernels();
+// (Re)builds the compact query keys of a finished index (after a build, a
+// clean, an import or a batched split).
+int make_query_keys(hsdl_index_impl* idx);
 // Host-side failure injection for tests (hsdl_debug_inject_failure): true if
 // the pass through `site` must fail; the error text is set.
 bool injected_failure(int site);

@@ -31,10 +31,10 @@ namespace {
 // plain kernel carries no prefetch code at all).
 // (Capping it at 32 registers for 64 resident warps per SM, against 38 and 48
 // warps, cut the rate from 322 M to 221 M q/s at n = 1M.)
-template <int G, bool PF>
+template <int G, bool PF, class KT, class F>
 __global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
                         const int32_t* __restrict__ qk, const int64_t* __restrict__ off,
-                        const uint64_t* __restrict__ key, int32_t* __restrict__ out, int ahead) {
+                        const KT* __restrict__ key, int32_t* __restrict__ out, int ahead, F f) {
   constexpr int Q = 32 / G;  // queries per warp step
   const int lane = lane_id(), grp = lane / G, gl = lane & (G - 1);
   const int64_t step = (((int64_t)gridDim.x * blockDim.x) >> 5) * Q;
@@ -46,23 +46,52 @@ __global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, c
     const int64_t q = base + grp;
     const bool active = q < nq;
     const int s = active ? qs[q] : 0, t = active ? qt[q] : 0, k = active ? qk[q] : 0;
-    const int32_t ans = group_query<G>(active, n, off, key, s, t, k);
+    const int32_t ans = group_query<G>(active, n, off, key, s, t, k, f);
     if (active && gl == 0) out[q] = ans;
   }
+}
+
+template <int G, bool PF, class KT, class F>
+int launch_query(hsdl_index_impl* idx, const KT* key, F f, int64_t nq, const int32_t* s, const int32_t* t,
+                 const int32_t* k, int32_t* out, cudaStream_t st) {
+  const int sms = device_sm_count();
+  const int threads = idx->q_threads;
+  const int64_t warps = (nq + (32 / G) - 1) / (32 / G);
+  int64_t blocks = (warps * 32 + threads - 1) / threads;
+  int64_t max_blocks = (int64_t)sms * resident_blocks(k_query<G, PF, KT, F>, threads);
+  k_query<G, PF, KT, F><<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p,
+                                                                                     key, out, idx->q_ahead, f);
+  HSDL_LAUNCHED();
+  return HSDL_OK;
 }
 
 template <int G, bool PF>
 int launch_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const int32_t* t, const int32_t* k, int32_t* out,
                  cudaStream_t st) {
-  const int sms = device_sm_count();
-  const int threads = idx->q_threads;
-  const int64_t warps = (nq + (32 / G) - 1) / (32 / G);
-  int64_t blocks = (warps * 32 + threads - 1) / threads;
-  int64_t max_blocks = (int64_t)sms * resident_blocks(k_query<G, PF>, threads);
-  k_query<G, PF><<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p,
-                                                                              idx->key.p, out, idx->q_ahead);
-  HSDL_LAUNCHED();
-  return HSDL_OK;
+  if (idx->key32.p) return launch_query<G, PF>(idx, idx->key32.p, idx->fmt32, nq, s, t, k, out, st);
+  return launch_query<G, PF>(idx, idx->key.p, Fmt64{}, nq, s, t, k, out, st);
+}
+
+// Largest distance field over the 8-byte keys.
+__global__ void k_max_dist(int64_t total, const uint64_t* __restrict__ key, unsigned int* out) {
+  uint32_t m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, lkey_dist(key[i]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane_id() == 0) atomicMax(out, m);
+}
+
+__global__ void k_pack32(int64_t total, const uint64_t* __restrict__ key, uint32_t* __restrict__ key32, Fmt32 f) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t x = key[i];
+    key32[i] = f.pack(lkey_hub(x), lkey_hop(x), lkey_dist(x));
+  }
+}
+
+int bits_for(uint32_t v) {  // bits needed to hold 0..v (at least 1)
+  int b = 1;
+  while (b < 32 && (v >> b) != 0) b++;
+  return b;
 }
 
 // Smallest index of a query naming a vertex outside [0, n) (stays all-ones if none).
@@ -86,15 +115,53 @@ int first_bad_query(hsdl_index_impl* idx, int64_t nq, const int32_t* s, const in
   return HSDL_OK;
 }
 
-int preload_query_kernels() {
+template <int G, bool PF>
+int preload_variant() {
   cudaFuncAttributes a;
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<8, false>));
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<8, true>));
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<16, false>));
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<16, true>));
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<32, false>));
-  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<32, true>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<G, PF, uint64_t, Fmt64>));
+  HSDL_CUDA(cudaFuncGetAttributes(&a, k_query<G, PF, uint32_t, Fmt32>));
+  return HSDL_OK;
+}
+
+int preload_query_kernels() {
+  HSDL_TRY((preload_variant<8, false>()));
+  HSDL_TRY((preload_variant<8, true>()));
+  HSDL_TRY((preload_variant<16, false>()));
+  HSDL_TRY((preload_variant<16, true>()));
+  HSDL_TRY((preload_variant<32, false>()));
+  HSDL_TRY((preload_variant<32, true>()));
+  cudaFuncAttributes a;
   HSDL_CUDA(cudaFuncGetAttributes(&a, k_first_bad_id));
+  return HSDL_OK;
+}
+
+// Builds the compact 4-byte query keys of a finished index when its ranges fit
+// (hub:H | hop:P | distance:D, see Fmt32), else releases them; the query
+// kernels use them when present.  Synchronises the index's stream.
+int make_query_keys(hsdl_index_impl* idx) {
+  cudaStream_t st = idx->stream;
+  idx->key32.release();
+  const int H = bits_for((uint32_t)std::max(0, idx->n - 1)), P = bits_for((uint32_t)idx->K);
+  const int D = 32 - H - P;
+  if (D < 1 || idx->total <= 0) return HSDL_OK;
+  const int sms = device_sm_count();
+  DevBuf<unsigned int> mx;
+  HSDL_TRY(mx.alloc(1, st));
+  HSDL_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned int), st));
+  k_max_dist<<<sms * 8, 256, 0, st>>>(idx->total, idx->key.p, mx.p);
+  HSDL_LAUNCHED();
+  unsigned int maxd = 0;
+  HSDL_CUDA(cudaMemcpyAsync(&maxd, mx.p, sizeof(maxd), cudaMemcpyDeviceToHost, st));
+  HSDL_CUDA(cudaStreamSynchronize(st));
+  mx.release();
+  if (D < 32 && (maxd >> D) != 0) return HSDL_OK;
+  Fmt32 f{(uint32_t)(P + D), (uint32_t)D};
+  HSDL_TRY(idx->key32.alloc(idx->total + kRowPad, st));
+  HSDL_CUDA(cudaMemsetAsync(idx->key32.p + idx->total, 0xFF, sizeof(uint32_t) * kRowPad, st));
+  k_pack32<<<sms * 8, 256, 0, st>>>(idx->total, idx->key.p, idx->key32.p, f);
+  HSDL_LAUNCHED();
+  idx->fmt32 = f;
+  HSDL_CUDA(cudaStreamSynchronize(st));
   return HSDL_OK;
 }
 

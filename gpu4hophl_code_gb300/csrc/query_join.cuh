@@ -23,12 +23,13 @@ namespace hsdl {
 // One lane's share of the merge-path join of label rows A (la labels) and B
 // (lb labels) under hop bound k >= 1, the merge split over a group of G lanes
 // (G = 8, 16 or 32; gl = lane index in the group); returns the lane's minimum
-// (INT_MAX if none).  Each label is one 8-byte key hub:32 | hop:4 |
-// distance:28, so hop and distance arrive with the hub id and a match needs
-// no dependent load (a layout with hub ids and hop|distance words in separate
-// arrays measured 238 M q/s against 322 M q/s for this one at n = 1M).
-template <int G>
-__device__ inline long long lane_merge(const uint64_t* A, int la, const uint64_t* B, int lb, int k, int gl) {
+// (INT_MAX if none).  Each label is one key - KT = uint64_t (hub:32 | hop:4 |
+// distance:28, format Fmt64) or uint32_t (the compact key, Fmt32) - so hop and
+// distance arrive with the hub id and a match needs no dependent load (a
+// layout with hub ids and hop|distance words in separate arrays measured
+// 238 M q/s against 322 M q/s for the 8-byte keys at n = 1M).
+template <int G, class KT, class F>
+__device__ inline long long lane_merge(const KT* A, int la, const KT* B, int lb, int k, int gl, F f) {
   long long best = INT_MAX;
   const int tot = la + lb;
   const int d0 = (int)(((int64_t)tot * gl) / G), d1 = (int)(((int64_t)tot * (gl + 1)) / G);
@@ -36,24 +37,25 @@ __device__ inline long long lane_merge(const uint64_t* A, int la, const uint64_t
   for (int span = la; span > 0; span >>= 1) {
     if (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if ((uint32_t)(A[mid] >> 32) <= (uint32_t)(B[d0 - 1 - mid] >> 32)) lo = mid + 1; else hi = mid;
+      if (f.hub(A[mid]) <= f.hub(B[d0 - 1 - mid])) lo = mid + 1; else hi = mid;
     }
   }
+  constexpr KT kEnd = (KT)~(KT)0;
   int ia = lo, ib = d0 - lo;
-  uint64_t wa = ia < la ? A[ia] : ~0ull;
-  uint64_t wb = ib < lb ? B[ib] : ~0ull;
+  KT wa = ia < la ? A[ia] : kEnd;
+  KT wb = ib < lb ? B[ib] : kEnd;
   for (int step = d0; step < d1; step++) {
-    const uint32_t ha = (uint32_t)(wa >> 32), hb = (uint32_t)(wb >> 32);
+    const uint32_t ha = f.hub(wa), hb = f.hub(wb);
     const bool take_a = ia < la && (ib >= lb || ha <= hb);
     if (take_a && ha == hb) {  // a common hub: B's run of it starts at ib
-      const int h1 = (int)lkey_hop(wa);
+      const int h1 = (int)f.hop(wa);
       if (h1 <= k) {
-        const long long da = lkey_dist(wa);
-        uint64_t xb = wb;
-        for (int p = ib; p < lb; xb = (++p < lb) ? B[p] : 0ull) {
-          if ((uint32_t)(xb >> 32) != ha) break;
-          if (h1 + (int)lkey_hop(xb) > k) break;  // rows are hop-sorted within a hub
-          const long long c = da + lkey_dist(xb);
+        const long long da = f.dist(wa);
+        KT xb = wb;
+        for (int p = ib; p < lb; xb = (++p < lb) ? B[p] : (KT)0) {
+          if (f.hub(xb) != ha) break;
+          if (h1 + (int)f.hop(xb) > k) break;  // rows are hop-sorted within a hub
+          const long long c = da + f.dist(xb);
           best = c < best ? c : best;
         }
       }
@@ -62,7 +64,7 @@ __device__ inline long long lane_merge(const uint64_t* A, int la, const uint64_t
     ib += take_a ? 0 : 1;
     const int at = take_a ? ia : ib;
     const int lim = take_a ? la : lb;
-    const uint64_t nxt = at < lim ? (take_a ? A : B)[at] : ~0ull;
+    const KT nxt = at < lim ? (take_a ? A : B)[at] : kEnd;
     wa = take_a ? nxt : wa;
     wb = take_a ? wb : nxt;
   }
@@ -89,16 +91,18 @@ __device__ inline void prefetch_l2(const void* p, uint32_t bytes) {
 }
 
 // Prefetches the 16-byte aligned spans holding rows s and t of the key array
-// into L2 (one lane issues).  The key array carries padding so the spans stay
-// inside the allocation.
-__device__ inline void prefetch_rows(const int64_t* __restrict__ off, const uint64_t* __restrict__ key, int32_t n,
-                                     int s, int t) {
+// (keys of KT) into L2 (one lane issues).  The key array carries padding so
+// the spans stay inside the allocation.
+template <class KT>
+__device__ inline void prefetch_rows(const int64_t* __restrict__ off, const KT* __restrict__ key, int32_t n, int s,
+                                     int t) {
   if (s < 0 || s >= n || t < 0 || t >= n || s == t) return;
+  constexpr int64_t per16 = 16 / sizeof(KT);
   const int64_t r[2] = {s, t};
 #pragma unroll
   for (int i = 0; i < 2; i++) {
-    int64_t a = off[r[i]] & ~(int64_t)1, b = (off[r[i] + 1] + 1) & ~(int64_t)1;
-    if (b > a) prefetch_l2(key + a, (uint32_t)(b - a) * 8u);
+    int64_t a = off[r[i]] & ~(per16 - 1), b = (off[r[i] + 1] + per16 - 1) & ~(per16 - 1);
+    if (b > a) prefetch_l2(key + a, (uint32_t)(b - a) * (uint32_t)sizeof(KT));
   }
 }
 
@@ -128,9 +132,9 @@ __device__ inline int32_t clamp_answer(long long best) { return best >= INT_MAX 
 // Each group of G lanes answers its own (s, t, k), rows read from global
 // memory; every lane of the warp must call it (inactive groups pass
 // active = false).  Every lane of a group returns the group's answer.
-template <int G>
+template <int G, class KT, class F>
 __device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __restrict__ off,
-                                      const uint64_t* __restrict__ key, int s, int t, int k) {
+                                      const KT* __restrict__ key, int s, int t, int k, F f) {
   int32_t ans = INT_MAX;
   long long best = INT_MAX;
   const bool trivial = !active || trivial_answer(n, s, t, k, &ans);
@@ -140,10 +144,16 @@ __device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __r
       int64_t x = a0; a0 = b0; b0 = x;
       x = a1; a1 = b1; b1 = x;
     }
-    best = lane_merge<G>(key + a0, (int)(a1 - a0), key + b0, (int)(b1 - b0), k, lane_id() & (G - 1));
+    best = lane_merge<G>(key + a0, (int)(a1 - a0), key + b0, (int)(b1 - b0), k, lane_id() & (G - 1), f);
   }
   best = group_min<G>(best);
   return trivial ? ans : clamp_answer(best);
+}
+
+template <int G>
+__device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __restrict__ off,
+                                      const uint64_t* __restrict__ key, int s, int t, int k) {
+  return group_query<G>(active, n, off, key, s, t, k, Fmt64{});
 }
 
 // The whole answer of one (s, t, k) by a full warp (every lane must call it).

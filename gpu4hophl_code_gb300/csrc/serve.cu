@@ -47,8 +47,11 @@ namespace {
 struct IndexDesc {
   const int64_t* off;
   const uint64_t* key;
+  const uint32_t* key32;  // compact query keys, or null
   int32_t n;
   int32_t valid;
+  uint32_t fmt;  // compact key format: hub_shift | dist_bits << 8
+  int32_t pad;
 };
 
 struct ServeReq {
@@ -168,13 +171,18 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       if (lane < cnt) r = ld_volatile_v4(ring + (mine_tk & mask));
       // every lane looks up its own request's index (and prefetches its rows
       // into L2 when the warp has several to answer)
-      IndexDesc d{nullptr, nullptr, 0, 0};
+      IndexDesc d{nullptr, nullptr, nullptr, 0, 0, 0, 0};
       if (lane < cnt && r.x >= 0 && r.x < max_idx) {
         d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
         d.key = (const uint64_t*)__ldcg((const unsigned long long*)&descs[r.x].key);
+        d.key32 = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].key32);
         d.n = __ldcg(&descs[r.x].n);
         d.valid = __ldcg(&descs[r.x].valid);
-        if (d.valid && cnt > Q) prefetch_rows(d.off, d.key, d.n, r.y, r.z);
+        d.fmt = __ldcg(&descs[r.x].fmt);
+        if (d.valid && cnt > Q) {
+          if (d.key32) prefetch_rows(d.off, d.key32, d.n, r.y, r.z);
+          else prefetch_rows(d.off, d.key, d.n, r.y, r.z);
+        }
       }
       if (lane < cnt && !d.valid) atomicAdd(&ctl->bad, 1ull);
       int32_t mine = INT_MAX;
@@ -188,8 +196,23 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
         const int k = __shfl_sync(0xffffffffu, r.w, j);
         const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
         const uint64_t* kr = (const uint64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.key, j);
+        const uint32_t* k32 = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.key32, j);
+        const uint32_t fmt = __shfl_sync(0xffffffffu, d.fmt, j);
         const int n = __shfl_sync(0xffffffffu, d.n, j);
-        const int32_t ans = group_query<G>(active, n, off, kr, s, t, k);
+        // groups of one warp may serve indexes of both key formats: each
+        // format's join runs, warp-wide, only if some group needs it
+        const bool is32 = k32 != nullptr;
+        const unsigned m32 = __ballot_sync(0xffffffffu, active && is32);
+        const unsigned m64 = __ballot_sync(0xffffffffu, active && !is32);
+        int32_t ans = INT_MAX;
+        if (m32) {
+          const int32_t a = group_query<G>(active && is32, n, off, k32, s, t, k, Fmt32{fmt & 0xFFu, fmt >> 8});
+          if (is32) ans = a;
+        }
+        if (m64) {
+          const int32_t a = group_query<G>(active && !is32, n, off, kr, s, t, k, Fmt64{});
+          if (!is32) ans = a;
+        }
         // lane j takes the answer of the group that served it
         const int src = (lane >= r0 && lane < r0 + Q) ? (lane - r0) * G : 0;
         const int32_t got = __shfl_sync(0xffffffffu, ans, src);
@@ -342,6 +365,8 @@ int write_desc(ServerImpl* S, int32_t gid, hsdl_index* idx, bool valid) {
   if (idx) {
     d.off = idx->off.p;
     d.key = idx->key.p;
+    d.key32 = idx->key32.p;
+    d.fmt = idx->fmt32.hub_shift | (idx->fmt32.dist_bits << 8);
     d.n = idx->n;
   }
   d.valid = valid ? 1 : 0;

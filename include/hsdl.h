@@ -58,6 +58,11 @@ int64_t hsdl_launch_count(void);
 #define HSDL_FAIL_STATIC_QUERY 1
 #define HSDL_FAIL_SITE_MAX 1
 int hsdl_debug_inject_failure(int32_t site, int32_t count);
+/* High-water mark, in bytes, of the current device's default memory pool
+ * (the pool the library's stream-ordered allocations draw from) since the last
+ * reset; reset != 0 first resets it to the memory in use.  For tests that
+ * check an entry point allocates nothing (no counterpart in the reference). */
+int hsdl_debug_pool_used_high(int64_t* bytes, int32_t reset);
 
 /* ------------------------------------------------------------------------
  * Host graphs: seeded synthetic generators and loaders.  The result is an
@@ -288,6 +293,10 @@ typedef struct hsdl_index_info {
   int64_t build_max_candidates;  /* longest candidate list of one wave */
   int32_t build_wave_splits;     /* waves split in two because their candidates outgrew the memory left */
   int32_t build_pool_chunks;     /* device allocations the label pool grew by */
+  int32_t query_key_bytes;       /* bytes per label the query joins stream: 4 when the index's ranges fit the
+                                    compact key hub:H | hop:P | distance:D (H = bits of n - 1, P = bits of K,
+                                    D = 32 - H - P), else 8 */
+  int32_t query_key_hub_bits;    /* H of the compact key (0 with 8-byte keys) */
 } hsdl_index_info;
 
 int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);

@@ -282,3 +282,25 @@ def test_build_rejects_weights_past_the_distance_limit():
     dev = H.Graph(g)
     with pytest.raises(H.HsdlError):
         H.Index.build(dev, 3)  # 3 * 1e8 >= 2^28
+
+
+@pytest.mark.parametrize("wmax,key_bytes", [(100, 4), (3_000_000, 8)])
+def test_query_key_formats_agree_with_the_oracle(orc, wmax, key_bytes):
+    """Indexes whose ranges fit get the compact 4-byte query keys (hub:H |
+    hop:P | distance:D); wide distances keep the 8-byte keys.  Both joins
+    answer exactly as the oracle."""
+    g = H.HostGraph.erdos_renyi(3000, 12000, 1, wmax, seed=61)
+    K = 5
+    dev, idx = gpu_build(g, K)
+    info = idx.info()
+    assert info["query_key_bytes"] == key_bytes
+    if key_bytes == 4:
+        assert info["query_key_hub_bits"] == 12
+    ref = orc.build(g, K, threads=1)
+    rng = np.random.default_rng(wmax)
+    s = rng.integers(0, g.n, 200000).astype(np.int32)
+    t = rng.integers(0, g.n, 200000).astype(np.int32)
+    k = rng.integers(-1, K + 2, 200000).astype(np.int32)
+    assert np.array_equal(idx.query(s, t, k), orc.query(ref, s, t, k))
+    idx.close()
+    dev.close()

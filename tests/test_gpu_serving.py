@@ -134,3 +134,31 @@ def test_wait_that_runs_out_reports_timeout():
     ref = H.Index.build(dev, 5)
     assert np.array_equal(srv.query(np.full(20000, gid, np.int32), s, t, k), ref.query(s, t, k))
     srv.close()
+
+
+@pytest.mark.parametrize("lanes", [32, 16, 8])
+def test_mixed_key_formats_in_one_warp(orc, lanes):
+    """One index whose ranges fit the compact 4-byte query keys and one whose
+    distances need the 8-byte keys, served together: with 16 or 8 lanes per
+    request a warp answers requests of both formats in one step."""
+    K = 5
+    small = H.HostGraph.erdos_renyi(1500, 6000, 1, 100, seed=45)
+    wide = H.HostGraph.erdos_renyi(1500, 6000, 1, 2_000_000, seed=46)
+    devs = [H.Graph(small), H.Graph(wide)]
+    idxs = [H.Index.build(d, K) for d in devs]
+    assert idxs[0].info()["query_key_bytes"] == 4 and idxs[1].info()["query_key_bytes"] == 8
+    srv = H.Server(idle_exit_s=0.2, lanes_per_query=lanes)
+    gids = [srv.add_index(ix) for ix in idxs]
+    rng = np.random.default_rng(9)
+    g = rng.integers(0, 2, 30000).astype(np.int32)
+    s = rng.integers(0, 1500, 30000).astype(np.int32)
+    t = rng.integers(0, 1500, 30000).astype(np.int32)
+    k = rng.integers(1, K + 1, 30000).astype(np.int32)
+    got = srv.query(np.asarray(gids, np.int32)[g], s, t, k)
+    for j, ix in enumerate(idxs):
+        sel = g == j
+        assert np.array_equal(got[sel], ix.query(s[sel], t[sel], k[sel]))
+    srv.close()
+    for ix, d in zip(idxs, devs):
+        ix.close()
+        d.close()

@@ -9,8 +9,7 @@ These tests call it through the C ABI: twice in a row against the allocating
 entry point hsdl_query_batch (integer answers: exact), after a failure
 injected on the host once work is queued (the lock must not be released while
 that work can still touch the shared array), with ids outside the index, and
-inside another stream's global-mode graph capture on the same thread (where
-CUDA refuses cudaMalloc: the call must still succeed).  Collected last so a
+against the device's memory accounting (no allocation, transient or held).  Collected last so a
 stop-at-first-failure run has already run every other test."""
 import ctypes as C
 
@@ -99,11 +98,11 @@ def test_ids_outside_the_index_are_rejected(built, index):
     assert rc == _native.HSDL_ERR_INVALID and "out of range at query 2" in _native.last_error()
 
 
-def test_call_succeeds_inside_a_global_mode_capture(built, index):
-    """While this thread captures another stream in global mode, CUDA refuses
-    calls that may allocate or synchronise the device; the static entry point
-    makes none.  Nothing is enqueued on the captured stream; the empty graph is
-    discarded."""
+def test_calls_allocate_no_device_memory(built, index):
+    """Two calls leave the default memory pool's high-water mark (every
+    stream-ordered allocation of the library draws from it) and the device's
+    free memory exactly as they were; the allocating entry point moves the
+    mark, which shows the check sees such allocations."""
     import torch
 
     from gpu4hophl_code_gb300 import _native
@@ -111,15 +110,20 @@ def test_call_succeeds_inside_a_global_mode_capture(built, index):
     g, idx = index
     fn = built.hsdl_query_batch_static
     rng = np.random.default_rng(7)
-    s, t, k = _batch(rng, g.n, 50_000)
-    want = idx.query(s, t, k)
+    s, t, k = _batch(rng, g.n, 400_000)
     got = np.zeros(len(s), np.int32)
-    side = torch.cuda.Stream()
-    graph = torch.cuda.CUDAGraph()
-    rc = None
-    with torch.cuda.graph(graph, stream=side, capture_error_mode="global"):
-        rc = fn(idx.handle, len(s), _p(s), _p(t), _p(k), _p(got))
-        err = _native.last_error()
-    del graph
-    assert rc == 0, err
+    assert fn(idx.handle, len(s), _p(s), _p(t), _p(k), _p(got)) == 0, _native.last_error()  # warm
+    torch.cuda.synchronize()
+    hw = C.c_int64()
+    assert built.hsdl_debug_pool_used_high(C.byref(hw), 1) == 0, _native.last_error()
+    base = hw.value
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        assert fn(idx.handle, len(s), _p(s), _p(t), _p(k), _p(got)) == 0, _native.last_error()
+    assert built.hsdl_debug_pool_used_high(C.byref(hw), 0) == 0
+    assert hw.value == base
+    assert torch.cuda.mem_get_info()[0] == free0
+    want = idx.query(s, t, k)  # hsdl_query_batch: stages in a stream-ordered allocation
     assert np.array_equal(got, want)
+    assert built.hsdl_debug_pool_used_high(C.byref(hw), 0) == 0
+    assert hw.value >= base + 16 * len(s)
