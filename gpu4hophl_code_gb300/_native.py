@@ -74,7 +74,7 @@ class hsdl_loadgen_result(C.Structure):
 
 
 class hsdl_query_loadgen_opts(C.Structure):
-    _fields_ = [("struct_size", C.c_int32), ("reserved", C.c_int32), ("n", C.c_int64), ("s", C.c_void_p),
+    _fields_ = [("struct_size", C.c_int32), ("max_batch", C.c_int32), ("n", C.c_int64), ("s", C.c_void_p),
                 ("t", C.c_void_p), ("k", C.c_void_p), ("answers", C.c_void_p), ("offered_qps", C.c_double),
                 ("seed", C.c_uint64), ("window_us", C.c_double)]
 

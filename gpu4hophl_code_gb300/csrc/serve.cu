@@ -865,13 +865,14 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
 // arrived are answered in batches by hsdl_query_batch (host arrays in, host
 // arrays out, one call at a time).  A batch is dispatched once the oldest
 // waiting request has waited window_us and the previous call has returned,
-// and takes every request that has arrived by then.  Latency runs from a
+// and takes every request that has arrived by then (at most max_batch).  Latency runs from a
 // request's scheduled arrival to the return of the call that answered it.
 int hsdl_query_loadgen(hsdl_index* idx, const hsdl_query_loadgen_opts* o, hsdl_loadgen_result* res) {
   SRV_ARG(idx && o && res, "null argument");
   SRV_ARG(o->struct_size == (int32_t)sizeof(hsdl_query_loadgen_opts), "hsdl_query_loadgen_opts.struct_size mismatch");
   const int64_t n = o->n;
-  SRV_ARG(n >= 1 && o->s && o->t && o->k && o->answers && o->window_us >= 0, "bad request arrays");
+  SRV_ARG(n >= 1 && o->s && o->t && o->k && o->answers && o->window_us >= 0 && o->max_batch >= 0,
+          "bad request arrays");
   std::vector<int64_t> arrive = poisson_arrivals_ns(n, o->offered_qps, o->seed);
   std::vector<int32_t> lat_ns((size_t)n);
   const int64_t window_ns = (int64_t)(o->window_us * 1e3);
@@ -883,6 +884,7 @@ int hsdl_query_loadgen(hsdl_index* idx, const hsdl_query_loadgen_opts* o, hsdl_l
     while ((now = mono_ns() - t_start) < dispatch) {
     }
     int64_t j = std::upper_bound(arrive.begin() + i, arrive.end(), now) - arrive.begin();
+    if (o->max_batch > 0) j = std::min<int64_t>(j, i + o->max_batch);
     HSDL_TRY(hsdl_query_batch(idx, j - i, o->s + i, o->t + i, o->k + i, o->answers + i));
     done = mono_ns() - t_start;
     for (int64_t r = i; r < j; r++) lat_ns[r] = (int32_t)std::min<int64_t>(INT32_MAX, done - arrive[r]);

@@ -338,7 +338,8 @@ class Index:
         check(lib().hsdl_query_batch_device(self._h, nq, C.c_void_p(d_s), C.c_void_p(d_t), C.c_void_p(d_k),
                                             C.c_void_p(d_out), C.c_void_p(stream) if stream else None))
 
-    def loadgen(self, s, t, k, offered_qps: float, window_us: float = 0.0, seed: int = 1, answers=None) -> dict:
+    def loadgen(self, s, t, k, offered_qps: float, window_us: float = 0.0, seed: int = 1, answers=None,
+                max_batch: int = 0) -> dict:
         """The plain path (hsdl_query_batch) under an open-loop Poisson stream
         of rate offered_qps, batched by arrival window (hsdl_query_loadgen).
         Pass pinned host arrays (e.g. torch pin_memory().numpy()) for a fair
@@ -354,6 +355,7 @@ class Index:
         o.offered_qps = offered_qps
         o.seed = seed
         o.window_us = window_us
+        o.max_batch = max_batch
         r = N.hsdl_loadgen_result()
         check(lib().hsdl_query_loadgen(self._h, C.byref(o), C.byref(r)))
         res = {f: getattr(r, f) for f, _ in N.hsdl_loadgen_result._fields_}

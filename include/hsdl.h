@@ -362,7 +362,7 @@ typedef struct hsdl_loadgen_result {
 /* The plain path under the same Poisson stream (hsdl_query_loadgen). */
 typedef struct hsdl_query_loadgen_opts {
   int32_t struct_size; /* sizeof(hsdl_query_loadgen_opts) */
-  int32_t reserved;
+  int32_t max_batch;   /* most requests per call (0 = no limit; 1 = one call per request) */
   int64_t n;           /* requests (all on the one index) */
   const int32_t* s;    /* source, target, hop bound per request (pinned host memory for a fair rate) */
   const int32_t* t;
