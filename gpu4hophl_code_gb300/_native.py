@@ -39,7 +39,7 @@ class hsdl_build_opts(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("clean", C.c_int32), ("first_wave", C.c_int32),
                 ("max_wave", C.c_int32), ("block_threads", C.c_int32), ("frontier_tile", C.c_int32),
                 ("prune_lanes", C.c_int32), ("prune_pairs", C.c_int32), ("generation", C.c_int32),
-                ("reserved", C.c_int32), ("device_budget_bytes", C.c_int64)]
+                ("prune_order", C.c_int32), ("device_budget_bytes", C.c_int64)]
 
 
 class hsdl_index_info(C.Structure):

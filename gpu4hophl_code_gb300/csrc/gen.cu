@@ -83,12 +83,12 @@ constexpr int kSlotFilterBits = 12;  // 1,024 / 4,096 / 16,384 bits: 2.23 / 2.19
 constexpr int kSlotFilterWords = (1 << kSlotFilterBits) / 32;
 constexpr int64_t kPoolEntryBytes = sizeof(uint64_t) + sizeof(int32_t);  // label key + parent
 // per candidate-list entry: C, both frontier buffers, and the found-label lists
-constexpr int64_t kListEntryBytes = sizeof(int2) + 2 * sizeof(int4) + 2 * sizeof(int32_t) + sizeof(uint64_t);
+constexpr int64_t kListEntryBytes = 2 * sizeof(int2) + 2 * sizeof(int4) + 2 * sizeof(int32_t) + sizeof(uint64_t);
 
 // An instantiated CUDA graph of one wave's hop kernels, keyed by the buffers
 // and sizes its launches name.
 struct HopGraph {
-  static constexpr int kKey = 11;
+  static constexpr int kKey = 12;
   cudaGraphExec_t exec = nullptr;
   uintptr_t key[kKey] = {};
   ~HopGraph() {
@@ -432,6 +432,98 @@ __global__ void __launch_bounds__(TPB) k_expand_heavy(SlotMap map, int32_t h, in
 
 // Closes hop h's candidate range.  On overflow the range stops at the list's
 // end; the wave is then rerun, so the truncated hop is never committed.
+// ---------------------------------------------------------------------------
+// hop round: candidates grouped by vertex range before the pruning join
+// ---------------------------------------------------------------------------
+// The expansion appends (slot, v) in frontier order, so consecutive pruning
+// groups read the rows of unrelated vertices, and a vertex that is a candidate
+// of many hubs of the wave has its row fetched from DRAM again for each.  One
+// radix partition by v >> shift (at most kPartBuckets ranges of consecutive
+// ids) puts every hub's candidates of a vertex range next to each other: the
+// joins then read a range's rows while L2 holds them.  Order inside a range is
+// arbitrary (the join's decisions do not depend on it).
+constexpr int kPartBuckets = 2048;
+constexpr int kPartTile = 8192;  // list entries a block partitions at a time
+
+__device__ inline void part_bounds(const Counters* ctr, int h, int64_t& c0, int64_t& c1) {
+  c0 = (int64_t)ctr->hop_c[h];
+  c1 = (int64_t)ctr->hop_c[h + 1];
+}
+
+// Range sizes of the hop's list (shared-memory histogram per tile, one global
+// atomic per non-empty range and tile).
+__global__ void __launch_bounds__(kThreads) k_part_count(const Counters* ctr, int h, const int2* __restrict__ C,
+                                                         unsigned int* __restrict__ bcnt, int shift) {
+  __shared__ unsigned int hist[kPartBuckets];
+  int64_t c0, c1;
+  part_bounds(ctr, h, c0, c1);
+  const int64_t tiles = (c1 - c0 + kPartTile - 1) / kPartTile;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const int64_t a = c0 + tile * kPartTile, e = min(c1, a + kPartTile);
+    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[C[i].y >> shift], 1u);
+    __syncthreads();
+    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x)
+      if (hist[b]) atomicAdd(&bcnt[b], hist[b]);
+    __syncthreads();
+  }
+}
+
+// Range starts (exclusive scan from the hop's list start); clears the counts
+// for the next hop.  One block of 1,024 threads.
+__global__ void k_part_scan(const Counters* ctr, int h, unsigned int* __restrict__ bcnt,
+                            unsigned long long* __restrict__ bcur) {
+  __shared__ int64_t warp_tot[32];
+  constexpr int per = kPartBuckets / 1024;
+  int64_t c0, c1;
+  part_bounds(ctr, h, c0, c1);
+  unsigned int v[per];
+  int64_t mine = 0;
+#pragma unroll
+  for (int j = 0; j < per; j++) {
+    v[j] = bcnt[threadIdx.x * per + j];
+    mine += v[j];
+  }
+  int64_t total;
+  int64_t x = block_exclusive_scan(mine, warp_tot, &total) + c0;
+#pragma unroll
+  for (int j = 0; j < per; j++) {
+    bcur[threadIdx.x * per + j] = (unsigned long long)x;
+    x += v[j];
+    bcnt[threadIdx.x * per + j] = 0;
+  }
+}
+
+// Scatters the hop's list into Cs by range, at the same list positions.
+__global__ void __launch_bounds__(kThreads) k_part_scatter(const Counters* ctr, int h, const int2* __restrict__ C,
+                                                           int2* __restrict__ Cs,
+                                                           unsigned long long* __restrict__ bcur, int shift) {
+  __shared__ unsigned int hist[kPartBuckets];
+  __shared__ unsigned long long base[kPartBuckets];
+  int64_t c0, c1;
+  part_bounds(ctr, h, c0, c1);
+  const int64_t tiles = (c1 - c0 + kPartTile - 1) / kPartTile;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const int64_t a = c0 + tile * kPartTile, e = min(c1, a + kPartTile);
+    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[C[i].y >> shift], 1u);
+    __syncthreads();
+    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) {
+      if (hist[b]) base[b] = atomicAdd(&bcur[b], (unsigned long long)hist[b]);
+      hist[b] = 0;
+    }
+    __syncthreads();
+    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) {
+      const int2 x = C[i];
+      const int b = x.y >> shift;
+      Cs[base[b] + atomicAdd(&hist[b], 1u)] = x;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_mark(Counters* ctr, int h, int64_t capC) {
   unsigned long long c = ctr->c_count;
   ctr->hop_c[h + 1] = c < (unsigned long long)capC ? c : (unsigned long long)capC;
@@ -865,7 +957,9 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<uint64_t*> d_ck;
   DevBuf<int32_t*> d_cp;
   DevBuf<unsigned long long> chunk_tail;
-  DevBuf<int2> Cl;
+  DevBuf<int2> Cl, Cs;  // the candidate list, and its copy grouped by vertex range
+  DevBuf<unsigned int> bcnt;
+  DevBuf<unsigned long long> bcur;
   DevBuf<int4> Fa, Fb;
   DevBuf<int32_t> wl_v, wl_par;
   DevBuf<uint64_t> wl_key;
@@ -883,7 +977,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   };
   auto release_all = [&]() {
     cand.release(); row_len.release(); cnt.release(); touched.release();
-    Cl.release(); Fa.release(); Fb.release(); wl_v.release();
+    Cl.release(); Cs.release(); bcnt.release(); bcur.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
     d_base.release(); filt.release(); wave_end_of.release(); tab_theta.release();
     release_pool();
@@ -943,8 +1037,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(add_chunk(first_chunk));
   const Rows rows{seg.p, d_ck.p, d_cp.p};
   int64_t capC = std::min<int64_t>(std::max<int64_t>(1 << 20, (int64_t)n * 4), c_limit);
+  const bool by_range = opts.prune_order == 0;
   auto alloc_lists = [&](int64_t c) -> int {
     HSDL_TRY(Cl.alloc(c, st));
+    if (by_range) HSDL_TRY(Cs.alloc(c, st));
     HSDL_TRY(Fa.alloc(c, st));
     HSDL_TRY(Fb.alloc(c, st));
     HSDL_TRY(wl_v.alloc(c, st));
@@ -953,6 +1049,15 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     return HSDL_OK;
   };
   HSDL_TRY(alloc_lists(capC));
+  // vertex ranges of the candidate partition: ids >> part_shift < kPartBuckets
+  int part_shift = 0;
+  while (((int64_t)(n - 1) >> part_shift) >= kPartBuckets) part_shift++;
+  if (by_range) {
+    HSDL_TRY(bcnt.alloc(kPartBuckets, st));
+    HSDL_TRY(bcur.alloc(kPartBuckets, st));
+    HSDL_CUDA(cudaMemsetAsync(bcnt.p, 0, (size_t)bcnt.bytes(), st));
+  }
+  const int g_part = sms * resident_blocks(k_part_scatter, kThreads);
   HSDL_TRY(tab_off.alloc(Wmax, st));
   HSDL_TRY(tab_cap.alloc(Wmax, st));
   HSDL_TRY(filt.alloc((int64_t)Wmax * kSlotFilterWords, st));
@@ -995,7 +1100,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 
   auto held = [&]() -> int64_t {
     return cand.bytes() + row_len.bytes() + cnt.bytes() + touched.bytes() + seg.bytes() +
-           pool_total * kPoolEntryBytes + Cl.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
+           pool_total * kPoolEntryBytes + Cl.bytes() + Cs.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
            wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() +
            filt.bytes() + chunk_map.bytes() + idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
   };
@@ -1027,8 +1132,17 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_CUDA(cudaGetLastError());
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());
+      if (by_range) {
+        k_part_count<<<g_part, kThreads, 0, st>>>(ctr.p, h, Cl.p, bcnt.p, part_shift);
+        HSDL_CUDA(cudaGetLastError());
+        k_part_scan<<<1, 1024, 0, st>>>(ctr.p, h, bcnt.p, bcur.p);
+        HSDL_CUDA(cudaGetLastError());
+        k_part_scatter<<<g_part, kThreads, 0, st>>>(ctr.p, h, Cl.p, Cs.p, bcur.p, part_shift);
+        HSDL_CUDA(cudaGetLastError());
+      }
+      const int2* Cp = by_range ? Cs.p : Cl.p;
 #define HSDL_PRUNE(G, P, SELF, GRID)                                                                        \
-  k_prune<G, P, SELF><<<GRID, kThreads, 0, st>>>(map, h, K, Cl.p, cand.p, rows, row_len.p, tab_off.p,       \
+  k_prune<G, P, SELF><<<GRID, kThreads, 0, st>>>(map, h, K, Cp, cand.p, rows, row_len.p, tab_off.p,       \
                                                  tab_cap.p, tab.p, stride, filt.p, tab_theta.p, Fout, wl_v.p, \
                                                  wl_key.p, wl_par.p, ctr.p)
       if (!rank_prune) {  // the 2023WWW search: candidates from earlier waves probe their self label
@@ -1053,10 +1167,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     const uintptr_t key[HopGraph::kKey] = {(uintptr_t)Cl.p, (uintptr_t)Fa.p, (uintptr_t)Fb.p,
                                            (uintptr_t)cand.p, (uintptr_t)tab.p, (uintptr_t)seg.p,
                                            (uintptr_t)wl_v.p, (uintptr_t)wl_key.p, (uintptr_t)wl_par.p,
-                                           (uintptr_t)capC, (uintptr_t)lanes};
+                                           (uintptr_t)capC, (uintptr_t)lanes, (uintptr_t)Cs.p};
     HSDL_TRY(hops.ensure(key, st, launch_hops));
     HSDL_CUDA(cudaGraphLaunch(hops.exec, st));
-    launch_counter().fetch_add(3 * K, std::memory_order_relaxed);
+    launch_counter().fetch_add((by_range ? 6 : 3) * K, std::memory_order_relaxed);
     return HSDL_OK;
   };
   for (size_t wv = 0; wv + 1 < bounds.size();) {

@@ -152,7 +152,9 @@ typedef struct hsdl_build_opts {
                              1 = the 2023WWW search (_2023WWW_thread_function, generation.h:226-370;
                              the reference's use_2023WWW_generation): no rank prune, so more labels
                              before the clean; the cleaned labels are the same */
-  int32_t reserved;       /* 0 */
+  int32_t prune_order;    /* 0 = each hop's candidates grouped by vertex-id range before the pruning join,
+                             so joins of one vertex's candidates read its row while L2 holds it (default);
+                             1 = expansion order.  Neither changes a label */
   int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
 } hsdl_build_opts;
 
