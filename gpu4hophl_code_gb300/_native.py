@@ -39,7 +39,8 @@ class hsdl_build_opts(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("clean", C.c_int32), ("first_wave", C.c_int32),
                 ("max_wave", C.c_int32), ("block_threads", C.c_int32), ("frontier_tile", C.c_int32),
                 ("prune_lanes", C.c_int32), ("prune_pairs", C.c_int32), ("generation", C.c_int32),
-                ("prune_order", C.c_int32), ("device_budget_bytes", C.c_int64)]
+                ("prune_order", C.c_int32), ("pool_key_bytes", C.c_int32), ("reserved", C.c_int32),
+                ("device_budget_bytes", C.c_int64)]
 
 
 class hsdl_index_info(C.Structure):
@@ -51,7 +52,8 @@ class hsdl_index_info(C.Structure):
                 ("work_candidates", C.c_int64), ("work_join_visible", C.c_int64),
                 ("build_peak_bytes", C.c_int64), ("build_pool_entries", C.c_int64),
                 ("build_max_candidates", C.c_int64), ("build_wave_splits", C.c_int32), ("build_pool_chunks", C.c_int32),
-                ("query_key_bytes", C.c_int32), ("query_key_hub_bits", C.c_int32)]
+                ("query_key_bytes", C.c_int32), ("query_key_hub_bits", C.c_int32),
+                ("build_pool_key_bytes", C.c_int32), ("reserved", C.c_int32)]
 
 
 class hsdl_serve_opts(C.Structure):

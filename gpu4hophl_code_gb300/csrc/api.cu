@@ -470,6 +470,7 @@ static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
   HSDL_CHECK_ARG(o->prune_pairs >= 0 && o->prune_pairs <= 2, "prune_pairs must be 0, 1 or 2");
   HSDL_CHECK_ARG(o->generation == 0 || o->generation == 1, "generation must be 0 (HSDL) or 1 (2023WWW)");
   HSDL_CHECK_ARG(o->prune_order == 0 || o->prune_order == 1, "prune_order must be 0 or 1");
+  HSDL_CHECK_ARG(o->pool_key_bytes == 0 || o->pool_key_bytes == 8, "pool_key_bytes must be 0 (auto) or 8");
   return HSDL_OK;
 }
 
@@ -641,6 +642,7 @@ int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info) {
   info->labels_after_clean = idx->after;
   info->device_bytes = idx->off.bytes() + idx->key.bytes() + idx->key32.bytes() + idx->par.bytes();
   info->query_key_bytes = idx->key32.p ? 4 : 8;
+  info->build_pool_key_bytes = idx->pool_key_bytes;
   info->query_key_hub_bits = idx->key32.p ? 32 - (int32_t)idx->fmt32.hub_shift : 0;
   info->time_generate_s = idx->t_gen;
   info->time_sort_s = idx->t_sort;

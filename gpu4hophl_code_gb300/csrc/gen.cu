@@ -62,18 +62,28 @@ __device__ inline int seg_of(int j) { return 31 - __clz((j >> 3) + 1); }
 __device__ inline int seg_first(int i) { return 8 * ((1 << i) - 1); }
 __device__ inline int segs_for(int64_t len) { return len <= 0 ? 0 : seg_of((int)(len - 1)) + 1; }
 
+// The pool's label keys are 8-byte keys (Fmt64: hub:32 | hop:4 | distance:28)
+// or, when the graph's ranges fit, 4-byte keys (Fmt32: hub:H | hop:P |
+// distance:D with H = bits of n - 1, P = bits of K + 1, every distance below
+// 2^D since it is at most K x the largest weight): a join's 16-byte load then
+// brings four labels instead of two.  In either format the all-ones key has a
+// hop field above K (never within a hop bound): it marks "no label".
+template <class F>
 struct Rows {
+  using KT = typename F::key_t;
   const int64_t* seg;        // [n][kSegs] segment references
-  uint64_t* const* ck;       // chunk -> label keys (hub:32 | hop:4 | distance:28)
+  void* const* ck;           // chunk -> label keys (KT)
   int32_t* const* cp;        // chunk -> parents
+  F f;                       // key format
   // where label j of row v lives: chunk and entry
   __device__ inline int64_t ref(int v, int j) const {
     const int i = seg_of(j);
     return __ldg(seg + (int64_t)v * kSegs + i) + (j - seg_first(i));
   }
-  __device__ inline uint64_t key(int v, int j) const {
+  __device__ inline KT* keys_of(int64_t r) const { return (KT*)ck[r >> 48] + (r & kEntryMask); }
+  __device__ inline KT key(int v, int j) const {
     const int64_t r = ref(v, j);
-    return __ldg(((const uint64_t* const*)ck)[r >> 48] + (r & kEntryMask));
+    return __ldg((const KT*)ck[r >> 48] + (r & kEntryMask));
   }
 };
 // Per-slot membership filter of the hub's own label hubs (4,096 bits): most
@@ -81,7 +91,6 @@ struct Rows {
 // a clear bit settles those with one load instead of a table probe sequence.
 constexpr int kSlotFilterBits = 12;  // 1,024 / 4,096 / 16,384 bits: 2.23 / 2.19 / 2.22 s of generation at n = 1M
 constexpr int kSlotFilterWords = (1 << kSlotFilterBits) / 32;
-constexpr int64_t kPoolEntryBytes = sizeof(uint64_t) + sizeof(int32_t);  // label key + parent
 // per candidate-list entry: C, both frontier buffers, and the found-label lists
 constexpr int64_t kListEntryBytes = 2 * sizeof(int2) + 2 * sizeof(int4) + 2 * sizeof(int32_t) + sizeof(uint64_t);
 
@@ -204,7 +213,8 @@ __global__ void k_table_size(int32_t W, int32_t s_hub, const int32_t* __restrict
 // Also records, per slot, the end of the wave of the hub's highest hub id
 // (tab_theta): labels of a vertex at or past it come from later waves, whose
 // hubs the wave's hub has no label for, so the pruning join stops there.
-__global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t* __restrict__ row_len,
+template <class F>
+__global__ void k_table_fill(int32_t W, int32_t s_hub, Rows<F> rows, const int32_t* __restrict__ row_len,
                              const int64_t* __restrict__ tab_off, const int32_t* __restrict__ tab_cap,
                              int32_t* __restrict__ tab, int stride, uint32_t* __restrict__ filt,
                              const int32_t* __restrict__ wave_end_of, int32_t* __restrict__ tab_theta) {
@@ -220,8 +230,8 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t*
     int len = row_len[hub];
     int32_t wmax = 0;
     for (int j = lane; j < len; j += 32) {
-      uint64_t k = rows.key(hub, j);
-      int32_t w = (int32_t)lkey_hub(k);
+      const typename F::key_t k = rows.key(hub, j);
+      int32_t w = (int32_t)rows.f.hub(k);
       wmax = max(wmax, w);
       const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)w);
       atomicOr(&filt[slot * kSlotFilterWords + (fb >> 5)], 1u << (fb & 31));
@@ -235,7 +245,7 @@ __global__ void k_table_fill(int32_t W, int32_t s_hub, Rows rows, const int32_t*
         }
         i = (i + 1) & mask;
       }
-      if (placed) atomicMin(&T[(int64_t)i * stride + 1 + lkey_hop(k)], (int32_t)lkey_dist(k));
+      if (placed) atomicMin(&T[(int64_t)i * stride + 1 + rows.f.hop(k)], (int32_t)rows.f.dist(k));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
@@ -575,10 +585,10 @@ __device__ inline void prune_flush(int4* kbuf, int& kn, SlotMap map, int32_t h, 
 // 32 gave generation 1.95 / 1.92 / 1.93 / 2.05 s at n = 1M (larger takes
 // leave a longer tail, smaller ones contend on the counter).
 constexpr int kPruneTake = 4;
-template <int G, int P, bool SELF = false>
+template <int G, int P, bool SELF, class F>
 __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
                                                     const int2* __restrict__ C, const uint64_t* __restrict__ cand,
-                                                    Rows rows, const int32_t* __restrict__ row_len,
+                                                    Rows<F> rows, const int32_t* __restrict__ row_len,
                                                     const int64_t* __restrict__ tab_off,
                                                     const int32_t* __restrict__ tab_cap,
                                                     const int32_t* __restrict__ tab, int stride,
@@ -628,42 +638,56 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         visible += (unsigned long long)len;
         // lane gl of the group holds the address of the row's segment gl, so
         // a label's address takes a shuffle instead of two dependent loads
-        const uint64_t* my_seg = nullptr;
+        using KT = typename F::key_t;
+        // labels per lane per load: 2 (one 16-byte load of 8-byte keys, one
+        // 8-byte load of 4-byte keys).  Four 4-byte keys per 16-byte load
+        // doubled the step (more labels read past the dominating one) and
+        // took 48 registers against 32: generation 2.28 s against 1.78 s.
+        constexpr int V = 2;
+        constexpr KT kNone = (KT)~(KT)0;          // hop field above K: never within the bound
+        const KT* my_seg = nullptr;
         if (gl < segs_for(len)) {
           const int64_t r = __ldg(rows.seg + (int64_t)v * kSegs + gl);
-          my_seg = ((const uint64_t* const*)rows.ck)[r >> 48] + (r & kEntryMask);
+          my_seg = (const KT*)rows.ck[r >> 48] + (r & kEntryMask);
         }
-        // Each lane takes two adjacent labels (one 16-byte load; pairs never
-        // straddle a segment, whose sizes and starts are even) and loads the
-        // next pair before it probes the current one.
-        auto load_pair = [&](int jp, uint64_t& k0, uint64_t& k1) {
+        // Each lane takes V adjacent labels (one load; segment sizes and
+        // starts are multiples of 8, so a load never straddles one) and loads
+        // the next ones before it probes the current ones.
+        auto load_vec = [&](int jp, KT (&k)[V]) {
           const int si = seg_of(min(jp, len - 1));
-          const uint64_t* sp =
-              (const uint64_t*)__shfl_sync(gmask, (unsigned long long)my_seg, si < G ? si : 0, G);
-          k0 = k1 = ~0ull;  // hop field 15: never within the bound
+          const KT* sp = (const KT*)__shfl_sync(gmask, (unsigned long long)my_seg, si < G ? si : 0, G);
+#pragma unroll
+          for (int x = 0; x < V; x++) k[x] = kNone;
           if (jp < len) {
             if (si < G) {
-              const uint4 x = __ldg((const uint4*)(sp + (jp - seg_first(si))));
-              k0 = ((uint64_t)x.y << 32) | x.x;
-              k1 = ((uint64_t)x.w << 32) | x.z;
+              if constexpr (sizeof(KT) == 8) {
+                const uint4 q4 = __ldg((const uint4*)(sp + (jp - seg_first(si))));
+                k[0] = (KT)(((uint64_t)q4.y << 32) | q4.x);
+                k[1] = (KT)(((uint64_t)q4.w << 32) | q4.z);
+              } else {
+                const uint2 q2 = __ldg((const uint2*)(sp + (jp - seg_first(si))));
+                k[0] = (KT)q2.x;
+                k[1] = (KT)q2.y;
+              }
             } else {
-              k0 = rows.key(v, jp);
-              if (jp + 1 < len) k1 = rows.key(v, jp + 1);
+#pragma unroll
+              for (int x = 0; x < V; x++)
+                if (jp + x < len) k[x] = rows.key(v, jp + x);
             }
-            if (jp + 1 >= len) k1 = ~0ull;
+#pragma unroll
+            for (int x = 1; x < V; x++)
+              if (jp + x >= len) k[x] = kNone;
           }
         };
         // the table probe of a label whose hub passed the slot's filter
-        auto probe = [&](uint64_t k) {
-          const int32_t w = (int32_t)lkey_hub(k);
-          const int h1 = (int)lkey_hop(k);
-          uint32_t ix = table_hash((uint32_t)w, mask);
+        auto probe = [&](uint32_t w, int h1, long long d1) {
+          uint32_t ix = table_hash(w, mask);
           for (int pr = 0; pr < cap; pr++) {
             const int32_t kk = T[(int64_t)ix * stride];
-            if (kk == w) {
+            if (kk == (int32_t)w) {
               const int32_t t = T[(int64_t)ix * stride + 1 + (h - h1)];
               if (t != kInf32) {
-                const long long c = (long long)lkey_dist(k) + t;
+                const long long c = d1 + t;
                 q = c < q ? c : q;
               }
               return;
@@ -678,33 +702,39 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         // added to the rows only when the index is finalised.
         if (SELF && v < s_hub && gl == 0) {
           const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)v);
-          if ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u) probe(lkey((uint32_t)v, 0, 0));
+          if ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u) probe((uint32_t)v, 0, 0);
         }
-        // a step covers 2 P G labels: lane gl takes the pairs at 2 gl + 2 G p
-        uint64_t a[2 * P];
+        // a step covers V P G labels: lane gl takes the vectors at V gl + V G p
+        KT a[P][V];
 #pragma unroll
-        for (int p = 0; p < P; p++) load_pair(2 * gl + 2 * G * p, a[2 * p], a[2 * p + 1]);
-        for (int j0 = 0; j0 < len; j0 += 2 * G * P) {
-          uint64_t b[2 * P];
+        for (int p = 0; p < P; p++) load_vec(V * gl + V * G * p, a[p]);
+        for (int j0 = 0; j0 < len; j0 += V * G * P) {
+          KT b[P][V];
 #pragma unroll
-          for (int p = 0; p < P; p++) load_pair(j0 + 2 * G * P + 2 * gl + 2 * G * p, b[2 * p], b[2 * p + 1]);
+          for (int p = 0; p < P; p++) load_vec(j0 + V * G * P + V * gl + V * G * p, b[p]);
           // the filter bit of each label's hub (0 for labels past the hop bound)
-          uint32_t f[2 * P];
+          uint32_t f[P][V];
 #pragma unroll
-          for (int x = 0; x < 2 * P; x++) {
-            const uint32_t fb = filter_bit<kSlotFilterBits>(lkey_hub(a[x]));
-            f[x] = (int)lkey_hop(a[x]) <= h ? (__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u : 0u;
-          }
+          for (int p = 0; p < P; p++)
+#pragma unroll
+            for (int x = 0; x < V; x++) {
+              const uint32_t fb = filter_bit<kSlotFilterBits>(rows.f.hub(a[p][x]));
+              f[p][x] = (int)rows.f.hop(a[p][x]) <= h ? (__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u : 0u;
+            }
           bool past = false;  // a label from a wave after the hub's last hub: the rest of the row is too
 #pragma unroll
-          for (int x = 0; x < 2 * P; x++) {
-            if (f[x]) probe(a[x]);
-            past |= lkey_hub(a[x]) >= theta;
-          }
-          scanned += (unsigned long long)min(2 * G * P, len - j0);
+          for (int p = 0; p < P; p++)
+#pragma unroll
+            for (int x = 0; x < V; x++) {
+              if (f[p][x]) probe(rows.f.hub(a[p][x]), (int)rows.f.hop(a[p][x]), (long long)rows.f.dist(a[p][x]));
+              past |= a[p][x] != kNone && rows.f.hub(a[p][x]) >= theta;
+            }
+          scanned += (unsigned long long)min(V * G * P, len - j0);
           if (__any_sync(gmask, q <= d || past)) break;  // dominated, or nothing further can match
 #pragma unroll
-          for (int x = 0; x < 2 * P; x++) a[x] = b[x];
+          for (int p = 0; p < P; p++)
+#pragma unroll
+            for (int x = 0; x < V; x++) a[p][x] = b[p][x];
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) {
@@ -776,15 +806,17 @@ __global__ void k_seg_alloc(const Counters* ctr, const int32_t* __restrict__ tou
   }
 }
 
+template <class F>
 __global__ void k_scatter(const Counters* ctr, const int32_t* __restrict__ wl_v, const uint64_t* __restrict__ wl_key,
-                          const int32_t* __restrict__ wl_par, int32_t* __restrict__ row_len, Rows rows) {
+                          const int32_t* __restrict__ wl_par, int32_t* __restrict__ row_len, Rows<F> rows) {
   int64_t total = (int64_t)ctr->wl_count;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
     const int v = wl_v[p];
     const int pos = atomicAdd(&row_len[v], 1);
     const int i = seg_of(pos);
     const int64_t r = rows.seg[(int64_t)v * kSegs + i] + (pos - seg_first(i));
-    rows.ck[r >> 48][r & kEntryMask] = wl_key[p];
+    const uint64_t x = wl_key[p];
+    *rows.keys_of(r) = rows.f.pack(lkey_hub(x), lkey_hop(x), lkey_dist(x));
     rows.cp[r >> 48][r & kEntryMask] = wl_par[p];
   }
 }
@@ -813,7 +845,8 @@ __global__ void k_final_len(int32_t n, const int32_t* __restrict__ row_len, int6
     flen[v] = (int64_t)row_len[v] + 1;
 }
 
-__global__ void k_final_copy(int32_t n, Rows rows, const int32_t* __restrict__ row_len,
+template <class F>
+__global__ void k_final_copy(int32_t n, Rows<F> rows, const int32_t* __restrict__ row_len,
                              const int64_t* __restrict__ foff, uint64_t* __restrict__ fkey,
                              int32_t* __restrict__ fpar) {
   int lane = lane_id();
@@ -824,7 +857,8 @@ __global__ void k_final_copy(int32_t n, Rows rows, const int32_t* __restrict__ r
     int len = row_len[v];
     for (int j = lane; j < len; j += 32) {
       const int64_t r = rows.ref((int)v, j);
-      fkey[dst + j] = rows.ck[r >> 48][r & kEntryMask];
+      const typename F::key_t x = *rows.keys_of(r);
+      fkey[dst + j] = lkey(rows.f.hub(x), rows.f.hop(x), rows.f.dist(x));
       fpar[dst + j] = rows.cp[r >> 48][r & kEntryMask];
     }
     if (lane == 0) {
@@ -952,9 +986,9 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<int32_t> row_len, cnt, touched;
   DevBuf<int64_t> seg;  // [n][kSegs] segment references of the committed rows
   // the label pool: chunks of keys and parents, and their device tables
-  std::vector<DevBuf<uint64_t>> chunk_keys;
+  std::vector<DevBuf<uint64_t>> chunk_keys;  // KT keys, stored in 8-byte words
   std::vector<DevBuf<int32_t>> chunk_par;
-  DevBuf<uint64_t*> d_ck;
+  DevBuf<void*> d_ck;
   DevBuf<int32_t*> d_cp;
   DevBuf<unsigned long long> chunk_tail;
   DevBuf<int2> Cl, Cs;  // the candidate list, and its copy grouped by vertex range
@@ -998,7 +1032,19 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(d_ck.alloc(kMaxChunks, st));
   HSDL_TRY(d_cp.alloc(kMaxChunks, st));
   HSDL_TRY(chunk_tail.alloc(1, st));
-  std::vector<uint64_t*> h_ck;
+  std::vector<void*> h_ck;
+  // pool key format: 4-byte keys (Fmt32) when every hub id, hop (<= K, with
+  // room for the all-ones "no label" hop above it) and distance (<= K x the
+  // largest weight) fit, unless the options ask for 8-byte keys
+  int fH = 1, fP = 1;
+  while (fH < 32 && ((uint32_t)std::max(0, n - 1) >> fH) != 0) fH++;
+  while (fP < 32 && ((uint32_t)(K + 1) >> fP) != 0) fP++;
+  const int fD = 32 - fH - fP;
+  const bool pool32 = opts.pool_key_bytes != 8 && fD >= 1 && fD < 31 &&
+                      (int64_t)K * std::max(1, g->max_w) < ((int64_t)1 << fD);
+  const Fmt32 f32{(uint32_t)(fP + fD), (uint32_t)std::max(fD, 1)};
+  const int64_t pool_entry_bytes = (pool32 ? 4 : 8) + (int64_t)sizeof(int32_t);  // label key + parent
+  idx->pool_key_bytes = pool32 ? 4 : 8;
   std::vector<int32_t*> h_cp;
   // Memory plan: the candidate lists of a wave take at most a quarter of the
   // budget (a wave needing more is split); the label pool takes what is left.
@@ -1013,7 +1059,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     const double per_v = 0.53 * std::sqrt((double)n) * std::max(1.0, deg / 10.0) * K / 5.0;
     first_chunk = std::max<int64_t>(first_chunk, (int64_t)(1.4 * per_v * n));
   }
-  first_chunk = std::max<int64_t>(1 << 16, std::min<int64_t>(first_chunk, budget / 3 / kPoolEntryBytes));
+  first_chunk = std::max<int64_t>(1 << 16, std::min<int64_t>(first_chunk, budget / 3 / pool_entry_bytes));
   int64_t pool_total = 0, chunk_cap = 0, chunk_used = 0;
   auto add_chunk = [&](int64_t entries) -> int {
     if ((int)chunk_keys.size() >= kMaxChunks) {
@@ -1022,11 +1068,11 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     }
     chunk_keys.emplace_back();
     chunk_par.emplace_back();
-    HSDL_TRY(chunk_keys.back().alloc(entries, st));
+    HSDL_TRY(chunk_keys.back().alloc(pool32 ? (entries + 1) / 2 : entries, st));
     HSDL_TRY(chunk_par.back().alloc(entries, st));
     h_ck.push_back(chunk_keys.back().p);
     h_cp.push_back(chunk_par.back().p);
-    HSDL_CUDA(cudaMemcpyAsync(d_ck.p, h_ck.data(), sizeof(uint64_t*) * h_ck.size(), cudaMemcpyHostToDevice, st));
+    HSDL_CUDA(cudaMemcpyAsync(d_ck.p, h_ck.data(), sizeof(void*) * h_ck.size(), cudaMemcpyHostToDevice, st));
     HSDL_CUDA(cudaMemcpyAsync(d_cp.p, h_cp.data(), sizeof(int32_t*) * h_cp.size(), cudaMemcpyHostToDevice, st));
     HSDL_CUDA(cudaMemsetAsync(chunk_tail.p, 0, sizeof(unsigned long long), st));
     pool_total += entries;
@@ -1035,7 +1081,8 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
     return HSDL_OK;
   };
   HSDL_TRY(add_chunk(first_chunk));
-  const Rows rows{seg.p, d_ck.p, d_cp.p};
+  const Rows<Fmt64> rows64{seg.p, d_ck.p, d_cp.p, Fmt64{}};
+  const Rows<Fmt32> rows32{seg.p, d_ck.p, d_cp.p, f32};
   int64_t capC = std::min<int64_t>(std::max<int64_t>(1 << 20, (int64_t)n * 4), c_limit);
   const bool by_range = opts.prune_order == 0;
   auto alloc_lists = [&](int64_t c) -> int {
@@ -1067,7 +1114,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(tab.alloc(tab_cap_entries * stride, st));
   HSDL_TRY(ctr.alloc(1, st));
   // grids of exactly one resident wave per kernel (grid-stride loops inside)
-  const int grid = sms * resident_blocks(k_scatter, 256);
+  const int grid = sms * resident_blocks(k_scatter<Fmt64>, 256);
   // tunables: threads per expansion block, frontier entries a block takes at
   // a time, lanes per pruning candidate (0 = chosen per wave from the mean
   // committed row length)
@@ -1084,15 +1131,19 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<int2> chunk_map;  // heavy expansion tiles, split into chunks
   HSDL_TRY(chunk_map.alloc(kExpandChunkCap, st));
   const int pairs = opts.prune_pairs == 2 ? 2 : 1;
-  const int g_prune8 = sms * (!rank_prune ? resident_blocks(k_prune<8, 1, true>, kThreads)
-                              : pairs == 2 ? resident_blocks(k_prune<8, 2>, kThreads)
-                                           : resident_blocks(k_prune<8, 1>, kThreads));
-  const int g_prune16 = sms * (!rank_prune ? resident_blocks(k_prune<16, 1, true>, kThreads)
-                               : pairs == 2 ? resident_blocks(k_prune<16, 2>, kThreads)
-                                            : resident_blocks(k_prune<16, 1>, kThreads));
-  const int g_prune32 = sms * (!rank_prune ? resident_blocks(k_prune<32, 1, true>, kThreads)
-                               : pairs == 2 ? resident_blocks(k_prune<32, 2>, kThreads)
-                                            : resident_blocks(k_prune<32, 1>, kThreads));
+  auto prune_blocks = [&](auto fmt, auto g) -> int {
+    using Fm = decltype(fmt);
+    constexpr int G = decltype(g)::value;
+    return sms * (!rank_prune ? resident_blocks(k_prune<G, 1, true, Fm>, kThreads)
+                  : pairs == 2 ? resident_blocks(k_prune<G, 2, false, Fm>, kThreads)
+                               : resident_blocks(k_prune<G, 1, false, Fm>, kThreads));
+  };
+  using G8 = std::integral_constant<int, 8>;
+  using G16 = std::integral_constant<int, 16>;
+  using G32 = std::integral_constant<int, 32>;
+  const int g_prune8 = pool32 ? prune_blocks(Fmt32{}, G8{}) : prune_blocks(Fmt64{}, G8{});
+  const int g_prune16 = pool32 ? prune_blocks(Fmt32{}, G16{}) : prune_blocks(Fmt64{}, G16{});
+  const int g_prune32 = pool32 ? prune_blocks(Fmt32{}, G32{}) : prune_blocks(Fmt64{}, G32{});
   int lanes = 32;
 
   Counters hc;
@@ -1100,7 +1151,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
 
   auto held = [&]() -> int64_t {
     return cand.bytes() + row_len.bytes() + cnt.bytes() + touched.bytes() + seg.bytes() +
-           pool_total * kPoolEntryBytes + Cl.bytes() + Cs.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
+           pool_total * pool_entry_bytes + Cl.bytes() + Cs.bytes() + Fa.bytes() + Fb.bytes() + wl_v.bytes() +
            wl_par.bytes() + wl_key.bytes() + tab_off.bytes() + tab_cap.bytes() + tab.bytes() + d_base.bytes() +
            filt.bytes() + chunk_map.bytes() + idx->off.bytes() + idx->key.bytes() + idx->par.bytes();
   };
@@ -1141,10 +1192,19 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
         HSDL_CUDA(cudaGetLastError());
       }
       const int2* Cp = by_range ? Cs.p : Cl.p;
-#define HSDL_PRUNE(G, P, SELF, GRID)                                                                        \
-  k_prune<G, P, SELF><<<GRID, kThreads, 0, st>>>(map, h, K, Cp, cand.p, rows, row_len.p, tab_off.p,       \
-                                                 tab_cap.p, tab.p, stride, filt.p, tab_theta.p, Fout, wl_v.p, \
-                                                 wl_key.p, wl_par.p, ctr.p)
+#define HSDL_PRUNE(G, P, SELF, GRID)                                                                          \
+  do {                                                                                                        \
+    if (pool32)                                                                                               \
+      k_prune<G, P, SELF, Fmt32><<<GRID, kThreads, 0, st>>>(map, h, K, Cp, cand.p, rows32, row_len.p,       \
+                                                            tab_off.p, tab_cap.p, tab.p, stride, filt.p,     \
+                                                            tab_theta.p, Fout, wl_v.p, wl_key.p, wl_par.p,   \
+                                                            ctr.p);                                          \
+    else                                                                                                      \
+      k_prune<G, P, SELF, Fmt64><<<GRID, kThreads, 0, st>>>(map, h, K, Cp, cand.p, rows64, row_len.p,       \
+                                                            tab_off.p, tab_cap.p, tab.p, stride, filt.p,     \
+                                                            tab_theta.p, Fout, wl_v.p, wl_key.p, wl_par.p,   \
+                                                            ctr.p);                                          \
+  } while (0)
       if (!rank_prune) {  // the 2023WWW search: candidates from earlier waves probe their self label
         if (lanes == 8) HSDL_PRUNE(8, 1, true, g_prune8);
         else if (lanes == 16) HSDL_PRUNE(16, 1, true, g_prune16);
@@ -1203,9 +1263,12 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       if (tab_need > 0) {
         HSDL_CUDA(cudaMemsetAsync(tab.p, 0x7F, (size_t)tab_need * stride * sizeof(int32_t), st));
         HSDL_CUDA(cudaMemsetAsync(filt.p, 0, (size_t)W * kSlotFilterWords * sizeof(uint32_t), st));
-        k_table_fill<<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(W, s_hub, rows, row_len.p, tab_off.p,
-                                                                   tab_cap.p, tab.p, stride, filt.p, wave_end_of.p,
-                                                                   tab_theta.p);
+        if (pool32)
+          k_table_fill<Fmt32><<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(
+              W, s_hub, rows32, row_len.p, tab_off.p, tab_cap.p, tab.p, stride, filt.p, wave_end_of.p, tab_theta.p);
+        else
+          k_table_fill<Fmt64><<<std::min(grid, (W + 7) / 8), 256, 0, st>>>(
+              W, s_hub, rows64, row_len.p, tab_off.p, tab_cap.p, tab.p, stride, filt.p, wave_end_of.p, tab_theta.p);
         HSDL_LAUNCHED();
         k_table_prefix<<<grid, 256, 0, st>>>(ctr.p, tab.p, stride, K);
         HSDL_LAUNCHED();
@@ -1275,7 +1338,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_LAUNCHED();
       chunk_used += need;
       idx->build_pool += need;
-      k_scatter<<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_len.p, rows);
+      if (pool32)
+        k_scatter<Fmt32><<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_len.p, rows32);
+      else
+        k_scatter<Fmt64><<<grid, 256, 0, st>>>(ctr.p, wl_v.p, wl_key.p, wl_par.p, row_len.p, rows64);
       HSDL_LAUNCHED();
       k_clear_cnt<<<grid, 256, 0, st>>>(ctr.p, touched.p, cnt.p);
       HSDL_LAUNCHED();
@@ -1315,7 +1381,10 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   HSDL_TRY(idx->key.alloc(total + kRowPad, st));
   HSDL_TRY(idx->par.alloc(total + kRowPad, st));
   note_peak();
-  k_final_copy<<<grid * 2, 256, 0, st>>>(n, rows, row_len.p, idx->off.p, idx->key.p, idx->par.p);
+  if (pool32)
+    k_final_copy<Fmt32><<<grid * 2, 256, 0, st>>>(n, rows32, row_len.p, idx->off.p, idx->key.p, idx->par.p);
+  else
+    k_final_copy<Fmt64><<<grid * 2, 256, 0, st>>>(n, rows64, row_len.p, idx->off.p, idx->key.p, idx->par.p);
   HSDL_LAUNCHED();
   flen.release();
   release_all();

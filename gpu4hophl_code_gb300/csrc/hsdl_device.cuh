@@ -53,11 +53,16 @@ __host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return hd_dist((uint
 // order, so the rows keep their sort; a join streams half the bytes of the
 // 8-byte keys.  Indexes whose ranges do not fit keep only the 8-byte keys.
 struct Fmt64 {
+  using key_t = uint64_t;
   __host__ __device__ uint32_t hub(uint64_t k) const { return (uint32_t)(k >> 32); }
   __host__ __device__ uint32_t hop(uint64_t k) const { return hd_hop((uint32_t)k); }
   __host__ __device__ uint32_t dist(uint64_t k) const { return hd_dist((uint32_t)k); }
+  __host__ __device__ uint64_t pack(uint32_t hub, uint32_t hop, uint32_t dist) const {
+    return ((uint64_t)hub << 32) | (uint64_t)hd_pack(hop, dist);
+  }
 };
 struct Fmt32 {
+  using key_t = uint32_t;
   uint32_t hub_shift;  // P + D
   uint32_t dist_bits;  // D
   __host__ __device__ uint32_t hub(uint32_t k) const { return k >> hub_shift; }

@@ -123,6 +123,7 @@ struct hsdl_index_impl {
   // device memory of the build
   int64_t build_peak = 0, build_pool = 0, build_max_cand = 0;
   int32_t wave_splits = 0, pool_chunks = 0;
+  int32_t pool_key_bytes = 8;  // bytes per key in the generation's label pool
   cudaStream_t stream = nullptr;
   std::vector<int64_t> h_off;  // host copy of offsets (path extraction, export)
 };

@@ -200,7 +200,7 @@ def generate_Group_CDLP(instance_graph, groups: list, MAX_GROUP_SIZE: int, max_i
 
 def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block_threads: int = 0,
                frontier_tile: int = 0, prune_lanes: int = 0, prune_pairs: int = 0, generation: int = 0,
-               prune_order: int = 0, device_budget_bytes: int = 0) -> N.hsdl_build_opts:
+               prune_order: int = 0, pool_key_bytes: int = 0, device_budget_bytes: int = 0) -> N.hsdl_build_opts:
     """generation: 0 = the HSDL search, 1 = the 2023WWW search (the
     reference's use_2023WWW_generation); the cleaned labels are the same.
     prune_order: 0 = each hop's candidates grouped by vertex range before the
@@ -216,6 +216,7 @@ def build_opts(clean: bool = True, first_wave: int = 1, max_wave: int = 0, block
     o.prune_pairs = prune_pairs
     o.generation = generation
     o.prune_order = prune_order
+    o.pool_key_bytes = pool_key_bytes
     o.device_budget_bytes = device_budget_bytes
     return o
 

@@ -155,6 +155,10 @@ typedef struct hsdl_build_opts {
   int32_t prune_order;    /* 0 = each hop's candidates grouped by vertex-id range before the pruning join,
                              so joins of one vertex's candidates read its row while L2 holds it (default);
                              1 = expansion order.  Neither changes a label */
+  int32_t pool_key_bytes; /* bytes per label key in the generation's label pool: 0 = 4 when every hub id,
+                             hop and distance fit a 32-bit key (hub:H | hop:P | distance:D), else 8;
+                             8 = always 8.  Changes no label */
+  int32_t reserved;       /* 0 */
   int64_t device_budget_bytes; /* 0 = no limit beyond free HBM */
 } hsdl_build_opts;
 
@@ -299,6 +303,8 @@ typedef struct hsdl_index_info {
                                     compact key hub:H | hop:P | distance:D (H = bits of n - 1, P = bits of K,
                                     D = 32 - H - P), else 8 */
   int32_t query_key_hub_bits;    /* H of the compact key (0 with 8-byte keys) */
+  int32_t build_pool_key_bytes;  /* bytes per label key in the generation's label pool (4 or 8) */
+  int32_t reserved;
 } hsdl_index_info;
 
 int hsdl_index_get_info(hsdl_index* idx, hsdl_index_info* info);

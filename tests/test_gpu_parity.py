@@ -55,19 +55,20 @@ def test_uncleaned_generation_matches_wave_oracle(orc, max_wave):
     assert np.array_equal(off2, canon.off) and np.array_equal(lab2, canon.lab)
 
 
-@pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes,prune_pairs,prune_order",
-                         [(128, 0, 8, 1, 0), (512, 4096, 16, 2, 1), (256, 1024, 32, 1, 0), (256, 0, 0, 2, 0),
-                          (256, 0, 8, 2, 1), (256, 0, 0, 1, 1)])
+@pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes,prune_pairs,prune_order,pool_key_bytes",
+                         [(128, 0, 8, 1, 0, 0), (512, 4096, 16, 2, 1, 0), (256, 1024, 32, 1, 0, 8),
+                          (256, 0, 0, 2, 0, 8), (256, 0, 8, 2, 1, 0), (256, 0, 0, 1, 1, 8), (256, 0, 16, 1, 0, 0)])
 def test_launch_shapes_do_not_change_labels(orc, block_threads, frontier_tile, prune_lanes, prune_pairs,
-                                            prune_order):
+                                            prune_order, pool_key_bytes):
     """The uncleaned superset depends on the wave schedule only; threads per
-    block, frontier tile, prune lanes and the order candidates are joined in
-    change the time, never a label."""
+    block, frontier tile, prune lanes, the order candidates are joined in and
+    the width of the label pool's keys change the time, never a label."""
     g = H.HostGraph.chung_lu(3000, 8, 2.2, 300, 1, 100, seed=22)
     K = 5
     dev, idx = gpu_build(g, K, clean=False, max_wave=64, block_threads=block_threads,
                          frontier_tile=frontier_tile, prune_lanes=prune_lanes, prune_pairs=prune_pairs,
-                         prune_order=prune_order)
+                         prune_order=prune_order, pool_key_bytes=pool_key_bytes)
+    assert idx.info()["build_pool_key_bytes"] == (pool_key_bytes or 4)
     off, lab = idx.export()
     ref = orc.build(g, K, threads=4, wave_bounds=H.wave_bounds(g.n, max_wave=64), clean=False)
     assert np.array_equal(off, ref.off) and np.array_equal(lab, ref.lab)
