@@ -469,7 +469,7 @@ static int resolve_opts(const hsdl_build_opts* in, hsdl_build_opts* o) {
                  "prune_lanes must be 0, 8, 16 or 32");
   HSDL_CHECK_ARG(o->prune_pairs >= 0 && o->prune_pairs <= 2, "prune_pairs must be 0, 1 or 2");
   HSDL_CHECK_ARG(o->generation == 0 || o->generation == 1, "generation must be 0 (HSDL) or 1 (2023WWW)");
-  HSDL_CHECK_ARG(o->prune_order == 0 || o->prune_order == 1, "prune_order must be 0 or 1");
+  HSDL_CHECK_ARG(o->prune_order >= 0 && o->prune_order <= 2, "prune_order must be 0, 1 or 2");
   HSDL_CHECK_ARG(o->pool_key_bytes == 0 || o->pool_key_bytes == 8, "pool_key_bytes must be 0 (auto) or 8");
   return HSDL_OK;
 }

@@ -144,6 +144,7 @@ struct Counters {
   unsigned long long take_p[16];  // pruning candidates taken
   unsigned long long heavy_chunks[16];  // chunks of heavy expansion tiles in the chunk map
   unsigned long long take_h[16];        // heavy chunks taken
+  unsigned long long take_t[16];        // slot tiles taken by the slot-tiled pruning join
   int s_hub;                      // first hub of the wave (read by the captured hop kernels)
   int pad32;
 };
@@ -452,7 +453,8 @@ __global__ void __launch_bounds__(TPB) k_expand_heavy(SlotMap map, int32_t h, in
 // ids) puts every hub's candidates of a vertex range next to each other: the
 // joins then read a range's rows while L2 holds them.  Order inside a range is
 // arbitrary (the join's decisions do not depend on it).
-constexpr int kPartBuckets = 2048;
+constexpr int kPartBuckets = 2048;  // vertex ranges of the by-range order
+constexpr int kPartMaxBuckets = 8192;  // buckets of either order (the by-slot order has one per slot)
 constexpr int kPartTile = 8192;  // list entries a block partitions at a time
 
 __device__ inline void part_bounds(const Counters* ctr, int h, int64_t& c0, int64_t& c1) {
@@ -460,74 +462,102 @@ __device__ inline void part_bounds(const Counters* ctr, int h, int64_t& c0, int6
   c1 = (int64_t)ctr->hop_c[h + 1];
 }
 
-// Range sizes of the hop's list (shared-memory histogram per tile, one global
-// atomic per non-empty range and tile).
+// Bucket of a candidate: its slot, or its vertex's id range.
+template <bool BY_SLOT>
+__device__ inline int part_bucket(int2 x, int shift) {
+  return BY_SLOT ? x.x : (x.y >> shift);
+}
+
+// Bucket sizes of the hop's list (shared-memory histogram of nb buckets per
+// tile, one global atomic per non-empty bucket and tile).
+template <bool BY_SLOT>
 __global__ void __launch_bounds__(kThreads) k_part_count(const Counters* ctr, int h, const int2* __restrict__ C,
-                                                         unsigned int* __restrict__ bcnt, int shift) {
-  __shared__ unsigned int hist[kPartBuckets];
+                                                         unsigned int* __restrict__ bcnt, int shift, int nb) {
+  extern __shared__ unsigned int hist[];
   int64_t c0, c1;
   part_bounds(ctr, h, c0, c1);
   const int64_t tiles = (c1 - c0 + kPartTile - 1) / kPartTile;
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) hist[b] = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) hist[b] = 0;
     __syncthreads();
     const int64_t a = c0 + tile * kPartTile, e = min(c1, a + kPartTile);
-    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[C[i].y >> shift], 1u);
+    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[part_bucket<BY_SLOT>(C[i], shift)], 1u);
     __syncthreads();
-    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
       if (hist[b]) atomicAdd(&bcnt[b], hist[b]);
     __syncthreads();
   }
 }
 
-// Range starts (exclusive scan from the hop's list start); clears the counts
-// for the next hop.  One block of 1,024 threads.
+// Bucket starts (exclusive scan from the hop's list start) into bcur; clears
+// the counts for the next hop.  With tile > 0 it also records each bucket's
+// start in bstart and its first work tile of `tile` candidates in tstart
+// (bstart[nb] = list end, tstart[nb] = tiles in all).  One block of 1,024
+// threads, nb <= kPartMaxBuckets.
 __global__ void k_part_scan(const Counters* ctr, int h, unsigned int* __restrict__ bcnt,
-                            unsigned long long* __restrict__ bcur) {
+                            unsigned long long* __restrict__ bcur, int nb, int tile,
+                            unsigned long long* __restrict__ bstart, unsigned long long* __restrict__ tstart) {
   __shared__ int64_t warp_tot[32];
-  constexpr int per = kPartBuckets / 1024;
+  constexpr int kPer = kPartMaxBuckets / 1024;
+  const int per = (nb + 1023) / 1024;
   int64_t c0, c1;
   part_bounds(ctr, h, c0, c1);
-  unsigned int v[per];
-  int64_t mine = 0;
+  unsigned int v[kPer];
+  int64_t mine = 0, mtiles = 0;
 #pragma unroll
-  for (int j = 0; j < per; j++) {
-    v[j] = bcnt[threadIdx.x * per + j];
+  for (int j = 0; j < kPer; j++) {
+    const int b = threadIdx.x * per + j;
+    v[j] = (j < per && b < nb) ? bcnt[b] : 0u;
     mine += v[j];
+    if (tile > 0) mtiles += (v[j] + tile - 1) / tile;
   }
-  int64_t total;
+  int64_t total, ttotal = 0;
   int64_t x = block_exclusive_scan(mine, warp_tot, &total) + c0;
+  int64_t tx = tile > 0 ? block_exclusive_scan(mtiles, warp_tot, &ttotal) : 0;
 #pragma unroll
-  for (int j = 0; j < per; j++) {
-    bcur[threadIdx.x * per + j] = (unsigned long long)x;
-    x += v[j];
-    bcnt[threadIdx.x * per + j] = 0;
+  for (int j = 0; j < kPer; j++) {
+    const int b = threadIdx.x * per + j;
+    if (j < per && b < nb) {
+      bcur[b] = (unsigned long long)x;
+      if (tile > 0) {
+        bstart[b] = (unsigned long long)x;
+        tstart[b] = (unsigned long long)tx;
+        tx += (v[j] + tile - 1) / tile;
+      }
+      x += v[j];
+      bcnt[b] = 0;
+    }
+  }
+  if (tile > 0 && threadIdx.x == 0) {
+    bstart[nb] = (unsigned long long)c1;
+    tstart[nb] = (unsigned long long)ttotal;
   }
 }
 
-// Scatters the hop's list into Cs by range, at the same list positions.
+// Scatters the hop's list into Cs by bucket, at the same list positions.
+template <bool BY_SLOT>
 __global__ void __launch_bounds__(kThreads) k_part_scatter(const Counters* ctr, int h, const int2* __restrict__ C,
                                                            int2* __restrict__ Cs,
-                                                           unsigned long long* __restrict__ bcur, int shift) {
-  __shared__ unsigned int hist[kPartBuckets];
-  __shared__ unsigned long long base[kPartBuckets];
+                                                           unsigned long long* __restrict__ bcur, int shift, int nb) {
+  extern __shared__ unsigned long long base[];  // nb bucket bases, then nb counters
+  unsigned int* hist = (unsigned int*)(base + nb);
   int64_t c0, c1;
   part_bounds(ctr, h, c0, c1);
   const int64_t tiles = (c1 - c0 + kPartTile - 1) / kPartTile;
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) hist[b] = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) hist[b] = 0;
     __syncthreads();
     const int64_t a = c0 + tile * kPartTile, e = min(c1, a + kPartTile);
-    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[C[i].y >> shift], 1u);
+    for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) atomicAdd(&hist[part_bucket<BY_SLOT>(C[i], shift)], 1u);
     __syncthreads();
-    for (int b = threadIdx.x; b < kPartBuckets; b += blockDim.x) {
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       if (hist[b]) base[b] = atomicAdd(&bcur[b], (unsigned long long)hist[b]);
       hist[b] = 0;
     }
     __syncthreads();
     for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x) {
       const int2 x = C[i];
-      const int b = x.y >> shift;
+      const int b = part_bucket<BY_SLOT>(x, shift);
       Cs[base[b] + atomicAdd(&hist[b], 1u)] = x;
     }
     __syncthreads();
@@ -585,55 +615,33 @@ __device__ inline void prune_flush(int4* kbuf, int& kn, SlotMap map, int32_t h, 
 // 32 gave generation 1.95 / 1.92 / 1.93 / 2.05 s at n = 1M (larger takes
 // leave a longer tail, smaller ones contend on the counter).
 constexpr int kPruneTake = 4;
-template <int G, int P, bool SELF, class F>
-__global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
-                                                    const int2* __restrict__ C, const uint64_t* __restrict__ cand,
-                                                    Rows<F> rows, const int32_t* __restrict__ row_len,
-                                                    const int64_t* __restrict__ tab_off,
-                                                    const int32_t* __restrict__ tab_cap,
-                                                    const int32_t* __restrict__ tab, int stride,
-                                                    const uint32_t* __restrict__ filt,
-                                                    const int32_t* __restrict__ tab_theta,
-                                                    int4* __restrict__ Fout, int32_t* __restrict__ wl_v,
-                                                    uint64_t* __restrict__ wl_key, int32_t* __restrict__ wl_par,
-                                                    Counters* ctr) {
-  constexpr int NG = 32 / G;
-  const int lane = lane_id();
-  const int gi = lane / G, gl = lane % G;
-  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (gi * G));
-  const int32_t s_hub = ctr->s_hub;
-  const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
-  unsigned long long scanned = 0, visible = 0;
-  __shared__ int4 s_kept[kThreads / 32][64];  // per-warp staging of kept candidates: slot, v, d, parent
-  int4* kbuf = s_kept[threadIdx.x >> 5];
-  int kn = 0;
-  for (;;) {
-    unsigned long long took = 0;
-    if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(kPruneTake * NG));
-    took = __shfl_sync(0xffffffffu, took, 0);
-    const int64_t i0 = c0 + (int64_t)took;
-    if (i0 >= c1) break;
-    const int64_t i1 = min(c1, i0 + kPruneTake * NG);
-    // (Loading the set-up of a group's 8 candidates up front, one lane each,
-    // doubled the registers of the 32-lane kernel and halved its occupancy:
-    // generation went from 2.28 s to 2.83 s at n = 1M.)
-    // warp-uniform trip count: a group past i1 decides nothing but stages with the warp
-    for (int64_t ib = i0; ib < i1; ib += NG) {
-      const int64_t i = ib + gi;
-      bool keep = false;
-      int4 kept = make_int4(0, 0, 0, 0);
-      if (i < i1) {
-      int2 e = C[i];
-      int slot = e.x, v = e.y;
-      uint64_t ck = cand[map.row(slot) + map.local(v)];
-      long long d = (long long)ckey_dist(ck);
-      long long q = LLONG_MAX;
-      int cap = tab_cap[slot];
-      if (cap > 0) {
-        const int32_t* T = tab + tab_off[slot] * stride;
-        const uint32_t* Fl = filt + (int64_t)slot * kSlotFilterWords;
-        const uint32_t theta = (uint32_t)tab_theta[slot];
-        uint32_t mask = (uint32_t)cap - 1;
+// The pruning query of one candidate e = (slot, v) by a group of G lanes (gl =
+// lane in the group, gmask = the group's lanes): the slot's hub table T (cap
+// slots of `stride` ints: hub id, then hop-prefix-min distances), its
+// membership filter Fl and stop threshold theta may live in global or shared
+// memory: with FLT_ANY the filter is read with plain (generic) loads, which
+// may name either space; without it, through the read-only global path
+// (ld.global.nc), which must not be given a shared-memory address.  Returns
+// true on lane 0 of the group when the candidate is kept; `kept` receives
+// (slot, v, d, parent).
+template <bool FLT_ANY>
+__device__ inline uint32_t filter_word(const uint32_t* Fl, uint32_t i) {
+  if constexpr (FLT_ANY) return Fl[i];
+  else return __ldg(Fl + i);
+}
+
+template <int G, int P, bool SELF, class F, bool FLT_ANY = false>
+__device__ inline bool prune_candidate(int2 e, int32_t h, int32_t s_hub, SlotMap map,
+                                       const uint64_t* __restrict__ cand, const Rows<F>& rows,
+                                       const int32_t* __restrict__ row_len, const int32_t* T, int cap, int stride,
+                                       const uint32_t* Fl, uint32_t theta, int gl, unsigned gmask,
+                                       unsigned long long& scanned, unsigned long long& visible, int4& kept) {
+  const int slot = e.x, v = e.y;
+  const uint64_t ck = cand[map.row(slot) + map.local(v)];
+  const long long d = (long long)ckey_dist(ck);
+  long long q = LLONG_MAX;
+  if (cap > 0) {
+        const uint32_t mask = (uint32_t)cap - 1;
         int len = row_len[v];
         visible += (unsigned long long)len;
         // lane gl of the group holds the address of the row's segment gl, so
@@ -702,7 +710,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
         // added to the rows only when the index is finalised.
         if (SELF && v < s_hub && gl == 0) {
           const uint32_t fb = filter_bit<kSlotFilterBits>((uint32_t)v);
-          if ((__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u) probe((uint32_t)v, 0, 0);
+          if ((filter_word<FLT_ANY>(Fl, fb >> 5) >> (fb & 31)) & 1u) probe((uint32_t)v, 0, 0);
         }
         // a step covers V P G labels: lane gl takes the vectors at V gl + V G p
         KT a[P][V];
@@ -719,7 +727,7 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
 #pragma unroll
             for (int x = 0; x < V; x++) {
               const uint32_t fb = filter_bit<kSlotFilterBits>(rows.f.hub(a[p][x]));
-              f[p][x] = (int)rows.f.hop(a[p][x]) <= h ? (__ldg(Fl + (fb >> 5)) >> (fb & 31)) & 1u : 0u;
+              f[p][x] = (int)rows.f.hop(a[p][x]) <= h ? (filter_word<FLT_ANY>(Fl, fb >> 5) >> (fb & 31)) & 1u : 0u;
             }
           bool past = false;  // a label from a wave after the hub's last hub: the rest of the row is too
 #pragma unroll
@@ -742,8 +750,53 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
           q = x < q ? x : q;
         }
       }
-      keep = d < q && gl == 0;
-      kept = make_int4(slot, v, (int)d, (int32_t)ckey_parent(ck));
+  kept = make_int4(slot, v, (int)d, (int32_t)ckey_parent(ck));
+  return d < q && gl == 0;
+}
+
+template <int G, int P, bool SELF, class F>
+__global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int32_t K,
+                                                    const int2* __restrict__ C, const uint64_t* __restrict__ cand,
+                                                    Rows<F> rows, const int32_t* __restrict__ row_len,
+                                                    const int64_t* __restrict__ tab_off,
+                                                    const int32_t* __restrict__ tab_cap,
+                                                    const int32_t* __restrict__ tab, int stride,
+                                                    const uint32_t* __restrict__ filt,
+                                                    const int32_t* __restrict__ tab_theta,
+                                                    int4* __restrict__ Fout, int32_t* __restrict__ wl_v,
+                                                    uint64_t* __restrict__ wl_key, int32_t* __restrict__ wl_par,
+                                                    Counters* ctr) {
+  constexpr int NG = 32 / G;
+  const int lane = lane_id();
+  const int gi = lane / G, gl = lane % G;
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (gi * G));
+  const int32_t s_hub = ctr->s_hub;
+  const int64_t c0 = (int64_t)ctr->hop_c[h], c1 = (int64_t)ctr->hop_c[h + 1];
+  unsigned long long scanned = 0, visible = 0;
+  __shared__ int4 s_kept[kThreads / 32][64];  // per-warp staging of kept candidates: slot, v, d, parent
+  int4* kbuf = s_kept[threadIdx.x >> 5];
+  int kn = 0;
+  for (;;) {
+    unsigned long long took = 0;
+    if (lane == 0) took = atomicAdd(&ctr->take_p[h], (unsigned long long)(kPruneTake * NG));
+    took = __shfl_sync(0xffffffffu, took, 0);
+    const int64_t i0 = c0 + (int64_t)took;
+    if (i0 >= c1) break;
+    const int64_t i1 = min(c1, i0 + kPruneTake * NG);
+    // (Loading the set-up of a group's 8 candidates up front, one lane each,
+    // doubled the registers of the 32-lane kernel and halved its occupancy:
+    // generation went from 2.28 s to 2.83 s at n = 1M.)
+    // warp-uniform trip count: a group past i1 decides nothing but stages with the warp
+    for (int64_t ib = i0; ib < i1; ib += NG) {
+      const int64_t i = ib + gi;
+      bool keep = false;
+      int4 kept = make_int4(0, 0, 0, 0);
+      if (i < i1) {
+      const int2 e = C[i];
+      const int cap = tab_cap[e.x];
+      keep = prune_candidate<G, P, SELF, F>(e, h, s_hub, map, cand, rows, row_len, tab + tab_off[e.x] * stride, cap,
+                                            stride, filt + (int64_t)e.x * kSlotFilterWords,
+                                            (uint32_t)tab_theta[e.x], gl, gmask, scanned, visible, kept);
       }
       // kept candidates become labels (and the next frontier) through the
       // warp's staging buffer: one atomic per 32 or more labels
@@ -756,6 +809,102 @@ __global__ void __launch_bounds__(kThreads) k_prune(SlotMap map, int32_t h, int3
   prune_flush(kbuf, kn, map, h, K, s_hub, Fout, wl_v, wl_key, wl_par, ctr);
   if (gl == 0 && scanned) atomicAdd(&ctr->reads, scanned);
   if (gl == 0 && visible) atomicAdd(&ctr->visible, visible);
+}
+
+// The pruning join with the hub's table in shared memory.  The hop's list is
+// grouped by slot and cut into tiles of up to kSlotTile candidates of one
+// slot; a block of kSlotThreads takes a tile, copies the slot's hub table and
+// membership filter into shared memory (when the table fits kSlotTableBytes),
+// and its warps join the tile's candidates, so a label's filter test and
+// table probe are shared-memory reads and only the label itself comes from
+// global memory.
+constexpr int kSlotThreads = 1024;
+constexpr int kSlotTile = 2048;
+constexpr int kSlotTableBytes = 64 * 1024;
+constexpr size_t kSlotSmem = kSlotTableBytes + sizeof(uint32_t) * kSlotFilterWords +
+                             sizeof(int4) * (kSlotThreads / 32) * 64;
+
+template <class F>
+__global__ void __launch_bounds__(kSlotThreads, 2)
+    k_prune_slot(SlotMap map, int32_t h, int32_t K, const int2* __restrict__ C, const uint64_t* __restrict__ cand,
+                 Rows<F> rows, const int32_t* __restrict__ row_len, const int64_t* __restrict__ tab_off,
+                 const int32_t* __restrict__ tab_cap, const int32_t* __restrict__ tab, int stride,
+                 const uint32_t* __restrict__ filt, const int32_t* __restrict__ tab_theta,
+                 const unsigned long long* __restrict__ bstart, const unsigned long long* __restrict__ tstart, int nb,
+                 int4* __restrict__ Fout, int32_t* __restrict__ wl_v, uint64_t* __restrict__ wl_key,
+                 int32_t* __restrict__ wl_par, Counters* ctr) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int32_t* s_tab = (int32_t*)smem;
+  uint32_t* s_filt = (uint32_t*)(smem + kSlotTableBytes);
+  int4* kbuf = (int4*)(smem + kSlotTableBytes + sizeof(uint32_t) * kSlotFilterWords) + (threadIdx.x >> 5) * 64;
+  __shared__ int64_t s_lo, s_hi;
+  __shared__ int s_slot, s_staged;
+  __shared__ unsigned long long s_take;
+  const int lane = lane_id();
+  const int32_t s_hub = ctr->s_hub;
+  const unsigned long long tiles = tstart[nb];
+  unsigned long long scanned = 0, visible = 0;
+  int kn = 0;
+  if (threadIdx.x == 0) s_staged = -1;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long t = atomicAdd(&ctr->take_t[h], 1ull);
+      int slot = -1;
+      if (t < tiles) {
+        int lo = 0, hi = nb;  // the last slot whose first tile is <= t
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (tstart[mid] <= t) lo = mid; else hi = mid;
+        }
+        slot = lo;
+        const int64_t b0 = (int64_t)bstart[slot], b1 = (int64_t)bstart[slot + 1];
+        s_lo = b0 + (int64_t)(t - tstart[slot]) * kSlotTile;
+        s_hi = min(b1, s_lo + kSlotTile);
+      }
+      s_slot = slot;
+      s_take = 0;
+    }
+    __syncthreads();
+    const int slot = s_slot;
+    if (slot < 0) break;
+    const int cap = tab_cap[slot];
+    const bool in_smem = cap > 0 && (int64_t)cap * stride * (int64_t)sizeof(int32_t) <= kSlotTableBytes;
+    if (in_smem && s_staged != slot) {
+      const int4* src = (const int4*)(tab + tab_off[slot] * stride);
+      int4* dst = (int4*)s_tab;
+      const int n16 = cap * stride / 4;  // stride is 8 or 16 ints
+      for (int j = threadIdx.x; j < n16; j += blockDim.x) dst[j] = __ldg(src + j);
+      const uint32_t* fsrc = filt + (int64_t)slot * kSlotFilterWords;
+      for (int j = threadIdx.x; j < kSlotFilterWords; j += blockDim.x) s_filt[j] = __ldg(fsrc + j);
+      __syncthreads();
+      if (threadIdx.x == 0) s_staged = slot;
+    }
+    const int32_t* T = in_smem ? s_tab : tab + tab_off[slot] * stride;
+    const uint32_t* Fl = in_smem ? s_filt : filt + (int64_t)slot * kSlotFilterWords;
+    const uint32_t theta = (uint32_t)tab_theta[slot];
+    const int64_t lo = s_lo, hi = s_hi;
+    for (;;) {
+      unsigned long long took = 0;
+      if (lane == 0) took = atomicAdd(&s_take, (unsigned long long)kPruneTake);
+      took = __shfl_sync(0xffffffffu, took, 0);
+      const int64_t i0 = lo + (int64_t)took;
+      if (i0 >= hi) break;
+      const int64_t i1 = min(hi, i0 + kPruneTake);
+      for (int64_t i = i0; i < i1; i++) {
+        int4 kept = make_int4(0, 0, 0, 0);
+        const bool keep = prune_candidate<32, 1, false, F, true>(C[i], h, s_hub, map, cand, rows, row_len, T, cap, stride,
+                                                           Fl, theta, lane, 0xffffffffu, scanned, visible, kept);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) kbuf[kn + __popc(m & ((1u << lane) - 1u))] = kept;
+        kn += __popc(m);
+        if (kn >= 32) prune_flush(kbuf, kn, map, h, K, s_hub, Fout, wl_v, wl_key, wl_par, ctr);
+      }
+    }
+    __syncthreads();  // the tile's joins are done before the table is replaced
+  }
+  prune_flush(kbuf, kn, map, h, K, s_hub, Fout, wl_v, wl_key, wl_par, ctr);
+  if (lane == 0 && scanned) atomicAdd(&ctr->reads, scanned);
+  if (lane == 0 && visible) atomicAdd(&ctr->visible, visible);
 }
 
 // ---------------------------------------------------------------------------
@@ -993,7 +1142,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   DevBuf<unsigned long long> chunk_tail;
   DevBuf<int2> Cl, Cs;  // the candidate list, and its copy grouped by vertex range
   DevBuf<unsigned int> bcnt;
-  DevBuf<unsigned long long> bcur;
+  DevBuf<unsigned long long> bcur, bstart, tstart;
   DevBuf<int4> Fa, Fb;
   DevBuf<int32_t> wl_v, wl_par;
   DevBuf<uint64_t> wl_key;
@@ -1011,7 +1160,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   };
   auto release_all = [&]() {
     cand.release(); row_len.release(); cnt.release(); touched.release();
-    Cl.release(); Cs.release(); bcnt.release(); bcur.release(); Fa.release(); Fb.release(); wl_v.release();
+    Cl.release(); Cs.release(); bcnt.release(); bcur.release(); bstart.release(); tstart.release(); Fa.release(); Fb.release(); wl_v.release();
     wl_par.release(); wl_key.release(); tab_off.release(); tab_cap.release(); tab.release(); ctr.release();
     d_base.release(); filt.release(); wave_end_of.release(); tab_theta.release();
     release_pool();
@@ -1084,10 +1233,15 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   const Rows<Fmt64> rows64{seg.p, d_ck.p, d_cp.p, Fmt64{}};
   const Rows<Fmt32> rows32{seg.p, d_ck.p, d_cp.p, f32};
   int64_t capC = std::min<int64_t>(std::max<int64_t>(1 << 20, (int64_t)n * 4), c_limit);
-  const bool by_range = opts.prune_order == 0;
+  // candidate order of the pruning join: 0 = grouped by vertex range, 2 =
+  // grouped by slot and joined with the hub table in shared memory (the
+  // HSDL search, waves of at most kPartMaxBuckets hubs, 32 lanes per
+  // candidate; other waves are grouped by vertex range), 1 = expansion order
+  const bool part = opts.prune_order != 1;
+  const bool by_slot_opt = opts.prune_order == 2 && rank_prune && Wmax <= kPartMaxBuckets;
   auto alloc_lists = [&](int64_t c) -> int {
     HSDL_TRY(Cl.alloc(c, st));
-    if (by_range) HSDL_TRY(Cs.alloc(c, st));
+    if (part) HSDL_TRY(Cs.alloc(c, st));
     HSDL_TRY(Fa.alloc(c, st));
     HSDL_TRY(Fb.alloc(c, st));
     HSDL_TRY(wl_v.alloc(c, st));
@@ -1099,12 +1253,28 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
   // vertex ranges of the candidate partition: ids >> part_shift < kPartBuckets
   int part_shift = 0;
   while (((int64_t)(n - 1) >> part_shift) >= kPartBuckets) part_shift++;
-  if (by_range) {
-    HSDL_TRY(bcnt.alloc(kPartBuckets, st));
-    HSDL_TRY(bcur.alloc(kPartBuckets, st));
+  if (part) {
+    HSDL_TRY(bcnt.alloc(kPartMaxBuckets, st));
+    HSDL_TRY(bcur.alloc(kPartMaxBuckets, st));
     HSDL_CUDA(cudaMemsetAsync(bcnt.p, 0, (size_t)bcnt.bytes(), st));
   }
-  const int g_part = sms * resident_blocks(k_part_scatter, kThreads);
+  if (by_slot_opt) {
+    HSDL_TRY(bstart.alloc((int64_t)Wmax + 1, st));
+    HSDL_TRY(tstart.alloc((int64_t)Wmax + 1, st));
+  }
+  const int nb_slot = std::max(1, Wmax);
+  const size_t smem_rc = sizeof(unsigned int) * kPartBuckets, smem_rs = 12 * (size_t)kPartBuckets;
+  const size_t smem_sc = sizeof(unsigned int) * nb_slot, smem_ss = 12 * (size_t)nb_slot;
+  HSDL_CUDA(cudaFuncSetAttribute(k_part_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(12 * kPartMaxBuckets)));
+  HSDL_CUDA(cudaFuncSetAttribute(k_part_count<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(4 * kPartMaxBuckets)));
+  HSDL_CUDA(cudaFuncSetAttribute(k_prune_slot<Fmt32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem));
+  HSDL_CUDA(cudaFuncSetAttribute(k_prune_slot<Fmt64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSlotSmem));
+  const int g_part = sms * resident_blocks(k_part_scatter<false>, kThreads, smem_rs);
+  const int g_part_slot = sms * resident_blocks(k_part_scatter<true>, kThreads, smem_ss);
+  const int g_slot = sms * (pool32 ? resident_blocks(k_prune_slot<Fmt32>, kSlotThreads, kSlotSmem)
+                                   : resident_blocks(k_prune_slot<Fmt64>, kSlotThreads, kSlotSmem));
   HSDL_TRY(tab_off.alloc(Wmax, st));
   HSDL_TRY(tab_cap.alloc(Wmax, st));
   HSDL_TRY(filt.alloc((int64_t)Wmax * kSlotFilterWords, st));
@@ -1183,15 +1353,35 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
       HSDL_CUDA(cudaGetLastError());
       k_mark<<<1, 1, 0, st>>>(ctr.p, h, capC);
       HSDL_CUDA(cudaGetLastError());
-      if (by_range) {
-        k_part_count<<<g_part, kThreads, 0, st>>>(ctr.p, h, Cl.p, bcnt.p, part_shift);
+      const bool slot_mode = by_slot_opt && lanes == 32;
+      if (slot_mode) {
+        k_part_count<true><<<g_part_slot, kThreads, smem_sc, st>>>(ctr.p, h, Cl.p, bcnt.p, 0, nb_slot);
         HSDL_CUDA(cudaGetLastError());
-        k_part_scan<<<1, 1024, 0, st>>>(ctr.p, h, bcnt.p, bcur.p);
+        k_part_scan<<<1, 1024, 0, st>>>(ctr.p, h, bcnt.p, bcur.p, nb_slot, kSlotTile, bstart.p, tstart.p);
         HSDL_CUDA(cudaGetLastError());
-        k_part_scatter<<<g_part, kThreads, 0, st>>>(ctr.p, h, Cl.p, Cs.p, bcur.p, part_shift);
+        k_part_scatter<true><<<g_part_slot, kThreads, smem_ss, st>>>(ctr.p, h, Cl.p, Cs.p, bcur.p, 0, nb_slot);
+        HSDL_CUDA(cudaGetLastError());
+        if (pool32)
+          k_prune_slot<Fmt32><<<g_slot, kSlotThreads, kSlotSmem, st>>>(
+              map, h, K, Cs.p, cand.p, rows32, row_len.p, tab_off.p, tab_cap.p, tab.p, stride, filt.p, tab_theta.p,
+              bstart.p, tstart.p, nb_slot, Fout, wl_v.p, wl_key.p, wl_par.p, ctr.p);
+        else
+          k_prune_slot<Fmt64><<<g_slot, kSlotThreads, kSlotSmem, st>>>(
+              map, h, K, Cs.p, cand.p, rows64, row_len.p, tab_off.p, tab_cap.p, tab.p, stride, filt.p, tab_theta.p,
+              bstart.p, tstart.p, nb_slot, Fout, wl_v.p, wl_key.p, wl_par.p, ctr.p);
+        HSDL_CUDA(cudaGetLastError());
+        continue;
+      }
+      if (part) {
+        k_part_count<false><<<g_part, kThreads, smem_rc, st>>>(ctr.p, h, Cl.p, bcnt.p, part_shift, kPartBuckets);
+        HSDL_CUDA(cudaGetLastError());
+        k_part_scan<<<1, 1024, 0, st>>>(ctr.p, h, bcnt.p, bcur.p, kPartBuckets, 0, nullptr, nullptr);
+        HSDL_CUDA(cudaGetLastError());
+        k_part_scatter<false><<<g_part, kThreads, smem_rs, st>>>(ctr.p, h, Cl.p, Cs.p, bcur.p, part_shift,
+                                                                 kPartBuckets);
         HSDL_CUDA(cudaGetLastError());
       }
-      const int2* Cp = by_range ? Cs.p : Cl.p;
+      const int2* Cp = part ? Cs.p : Cl.p;
 #define HSDL_PRUNE(G, P, SELF, GRID)                                                                          \
   do {                                                                                                        \
     if (pool32)                                                                                               \
@@ -1230,7 +1420,7 @@ int build_index(hsdl_graph_impl* g, int32_t K, const hsdl_build_opts& opts, hsdl
                                            (uintptr_t)capC, (uintptr_t)lanes, (uintptr_t)Cs.p};
     HSDL_TRY(hops.ensure(key, st, launch_hops));
     HSDL_CUDA(cudaGraphLaunch(hops.exec, st));
-    launch_counter().fetch_add((by_range ? 6 : 3) * K, std::memory_order_relaxed);
+    launch_counter().fetch_add((part ? 6 : 3) * K, std::memory_order_relaxed);
     return HSDL_OK;
   };
   for (size_t wv = 0; wv + 1 < bounds.size();) {

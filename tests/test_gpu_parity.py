@@ -57,7 +57,8 @@ def test_uncleaned_generation_matches_wave_oracle(orc, max_wave):
 
 @pytest.mark.parametrize("block_threads,frontier_tile,prune_lanes,prune_pairs,prune_order,pool_key_bytes",
                          [(128, 0, 8, 1, 0, 0), (512, 4096, 16, 2, 1, 0), (256, 1024, 32, 1, 0, 8),
-                          (256, 0, 0, 2, 0, 8), (256, 0, 8, 2, 1, 0), (256, 0, 0, 1, 1, 8), (256, 0, 16, 1, 0, 0)])
+                          (256, 0, 0, 2, 0, 8), (256, 0, 8, 2, 1, 0), (256, 0, 0, 1, 1, 8), (256, 0, 16, 1, 0, 0),
+                          (256, 0, 32, 1, 2, 0), (256, 0, 32, 1, 2, 8), (256, 0, 0, 1, 2, 0)])
 def test_launch_shapes_do_not_change_labels(orc, block_threads, frontier_tile, prune_lanes, prune_pairs,
                                             prune_order, pool_key_bytes):
     """The uncleaned superset depends on the wave schedule only; threads per
