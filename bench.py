@@ -257,6 +257,19 @@ def captured_traffic(args) -> dict | None:
     return rec
 
 
+def work_summary(info: dict) -> dict:
+    """The build's device work counters and the ratios that explain its time:
+    pruning-join label reads per candidate (the join's dominant cost grows with
+    the committed rows it scans), candidates per generated label."""
+    cand = max(1, info["work_candidates"])
+    return {k: info[k] for k in ("work_relaxations", "work_candidates", "work_join_reads", "work_join_visible",
+                                 "work_labels_written", "work_clean_reads")} | {
+        "join_reads_per_candidate": round(info["work_join_reads"] / cand, 1),
+        "visible_per_candidate": round(info["work_join_visible"] / cand, 1),
+        "candidates_per_label": round(cand / max(1, info["work_labels_written"]), 2),
+        "mean_row_final": round(info["labels"] / max(1, info["n"]), 1)}
+
+
 def build_algorithmic_bytes(info: dict) -> int:
     """Bytes the build must move, from the work the device counted: per
     relaxation an 8-byte adjacency entry and an 8-byte candidate key; per
@@ -591,9 +604,7 @@ def run_ours(args, dist, rank, world, local):
                       "roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": peak,
                                    "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / peak, 4),
                                    "algorithmic_bytes": build_bytes, "model": "bytes the kernels read and write",
-                                   "work": {k: info[k] for k in ("work_relaxations", "work_join_reads",
-                                                                 "work_join_visible", "work_labels_written",
-                                                                 "work_clean_reads", "work_candidates")}},
+                                   "work": work_summary(info)},
                       "roofline_generation_scope_model": {
                           "bound": "hbm", "bytes": gen_scope_bytes, "seconds": round(info["time_generate_s"], 3),
                           "achieved": round(gen_scope_bytes / info["time_generate_s"] / 1e9, 1), "peak": peak,
@@ -719,7 +730,23 @@ def run_batched(args, dist, rank, world, local):
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
         if step == args.steps - 1:
-            labels = int(sum(ix.info()["labels"] for ix in idxs))
+            infos = [ix.info() for ix in idxs]
+            labels = int(sum(i["labels"] for i in infos))
+            # every graph of a sub-batch carries the sub-batch's build record
+            subs = {}
+            for i in infos:
+                key = (i["time_generate_s"], i["waves"], i["work_candidates"], i["work_join_reads"])
+                subs.setdefault(key, i)
+            sub_info = {"sub_batches": len(subs), "waves": int(sum(i["waves"] for i in subs.values())),
+                        "generate_s": round(sum(i["time_generate_s"] for i in subs.values()), 3),
+                        "sort_s": round(sum(i["time_sort_s"] for i in subs.values()), 3),
+                        "clean_s": round(sum(i["time_clean_s"] for i in subs.values()), 3),
+                        "pool_key_bytes": sorted({i["build_pool_key_bytes"] for i in subs.values()})}
+            tot = {k: sum(i[k] for i in subs.values()) for k in ("work_relaxations", "work_candidates",
+                                                                  "work_join_reads", "work_join_visible",
+                                                                  "work_labels_written", "work_clean_reads")}
+            tot["labels"], tot["n"] = labels, total_n
+            sub_info["work"] = work_summary(tot)
             rng = np.random.default_rng(5)
             for i in rng.choice(len(graphs), size=min(16, len(graphs)), replace=False):
                 dev = H.Graph(graphs[i])
@@ -746,6 +773,7 @@ def run_batched(args, dist, rank, world, local):
                                "w uniform [1, 1000], K in {3..6}",
                    "graphs": args.graphs, "vertices": total_n, "edges": total_m, "parallelism": f"replicas{world}"},
         "build_s": round(best, 3), "labels": labels, "labels_per_s": round(labels / best, 1),
+        "sub_batches": sub_info,
         "autotune": {"shapes": shapes, "seconds": round(tune_s, 2), "trials": tuned["trials"]},
         "default_shapes_build_s": round(default_s, 3), "host_graph_gen_s": round(gen_s, 1),
         "parity": "16 graphs bit-exact vs their single builds",
@@ -814,7 +842,9 @@ def run_stress(args, dist, rank, world, local):
                   "generate_s": round(info["time_generate_s"], 2), "clean_s": round(info["time_clean_s"], 2),
                   "labels": info["labels"], "labels_before_clean": info["labels_before_clean"],
                   "index_bytes": info["device_bytes"], "peak_bytes": info["build_peak_bytes"],
-                  "wave_splits": info["build_wave_splits"], "pool_chunks": info["build_pool_chunks"]},
+                  "wave_splits": info["build_wave_splits"], "pool_chunks": info["build_pool_chunks"],
+                  "waves": info["waves"], "labels_per_s": round(info["labels"] / build_s, 1),
+                  "work": work_summary(info)},
         "parity": "serving answers == batched-path answers on all queries",
     }
 

@@ -260,6 +260,13 @@ int build_sub_batch(const std::vector<GraphIn>& G, const std::vector<int32_t>& m
       // the sub-batch's build, shared by its graphs
       x->build_peak = uidx->build_peak;
       x->build_pool = uidx->build_pool;
+      x->pool_key_bytes = uidx->pool_key_bytes;
+      x->work_relax = uidx->work_relax;
+      x->work_join_reads = uidx->work_join_reads;
+      x->work_join_visible = uidx->work_join_visible;
+      x->work_labels_written = uidx->work_labels_written;
+      x->work_candidates = uidx->work_candidates;
+      x->work_clean_reads = uidx->work_clean_reads;
       x->build_max_cand = uidx->build_max_cand;
       x->wave_splits = uidx->wave_splits;
       x->pool_chunks = uidx->pool_chunks;
