@@ -125,7 +125,15 @@ struct Index {
   int64_t before = 0, after = 0;
   // work counters of the last generation
   int64_t popped = 0, relaxed = 0, query_reads = 0;
+  int64_t hubs_searched = 0;  // hubs whose search ran (n unless a time cap stopped the generation)
 };
+
+// Time cap of the generation with the reference schedule (seconds, 0 = none):
+// the watchdog pattern of the reference's experiment drivers
+// (GPU4HSDL_EXP/CPU_HopHL/include/HBPLL/hop_constrained_two_hop_labels_generation.h:67-83):
+// once it passes, workers start no further hub; the labels of the hubs
+// searched so far are sorted and cleaned as usual.
+double g_time_cap_s = 0;
 
 // Per-worker scratch of the generation.
 struct Scratch {
@@ -527,13 +535,17 @@ void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, 
     // visible as soon as they are written (generation.h:586-595)
     std::vector<std::mutex> mtx(n);
     std::atomic<int> next{0};
+    std::atomic<int64_t> searched{0};
     std::vector<Index> stats(threads);
+    const double cap = g_time_cap_s;
     auto worker = [&](int tid) {
       Scratch S(n, K);
       std::vector<Label> snap;
       for (;;) {
+        if (cap > 0 && now_s() - t0 > cap) break;
         int hub = next.fetch_add(1);
         if (hub >= n) break;
+        searched.fetch_add(1);
         {
           std::lock_guard<std::mutex> lk(mtx[hub]);
           I->L[hub].push_back(Label{hub, hub, 0, 0});  // self label (generation.h:83-92)
@@ -558,6 +570,8 @@ void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, 
       Scratch S(n, K);
       std::vector<Label> snap;
       for (int hub = 0; hub < n; hub++) {
+        if (cap > 0 && now_s() - t0 > cap) break;
+        searched.fetch_add(1);
         I->L[hub].push_back(Label{hub, hub, 0, 0});
         snap.assign(I->L[hub].begin(), I->L[hub].end() - 1);
         hub_search(
@@ -574,6 +588,7 @@ void* orc_build(int n, const int64_t* rp, const int32_t* col, const int32_t* w, 
       I->relaxed += s.relaxed;
       I->query_reads += s.query_reads;
     }
+    I->hubs_searched = searched.load();
   }
   if (variant != 1 && waves) {
     // in wave mode the self label is emitted by no search; add it per vertex
@@ -630,6 +645,9 @@ void orc_clean(void* h, int threads, int mode) {
   for (auto& x : I->L) I->after += (int64_t)x.size();
 }
 
+// Time cap (seconds, 0 = none) of later builds with the reference schedule.
+void orc_set_time_cap(double seconds) { g_time_cap_s = seconds > 0 ? seconds : 0; }
+
 int64_t orc_size(void* h) {
   Index* I = (Index*)h;
   int64_t t = 0;
@@ -637,7 +655,7 @@ int64_t orc_size(void* h) {
   return t;
 }
 
-// info[0..5] = t_gen, t_sort, t_clean, before, after, 0 ; work[0..2] = popped, relaxed, query_reads
+// info[0..5] = t_gen, t_sort, t_clean, before, after, hubs searched ; work[0..2] = popped, relaxed, query_reads
 void orc_info(void* h, double* info, int64_t* work) {
   Index* I = (Index*)h;
   info[0] = I->t_gen;
@@ -645,7 +663,7 @@ void orc_info(void* h, double* info, int64_t* work) {
   info[2] = I->t_clean;
   info[3] = (double)I->before;
   info[4] = (double)I->after;
-  info[5] = 0;
+  info[5] = (double)I->hubs_searched;
   if (work) {
     work[0] = I->popped;
     work[1] = I->relaxed;

@@ -101,6 +101,7 @@ class Oracle:
         L.orc_lp_group.argtypes = [i32, vp, vp, i32, i32, vp, vp]
         L.orc_lp_assemble.restype = i32
         L.orc_lp_assemble.argtypes = [i32, vp, vp, i32, vp]
+        L.orc_set_time_cap.argtypes = [C.c_double]
         L.orc_gen_chung_lu.restype = vp
         L.orc_gen_chung_lu.argtypes = [i32, C.c_double, C.c_double, C.c_double, i32, i32, C.c_uint64, vp]
         L.orc_graph_copy.argtypes = [vp, vp, vp, vp]
@@ -133,6 +134,7 @@ class Oracle:
         self.L.orc_export(h, _p(off), _p(lab))
         return Labels(off, lab[:tot], {"t_gen": info[0], "t_sort": info[1], "t_clean": info[2],
                                        "before": int(info[3]), "after": int(info[4]),
+                                       "hubs_searched": int(info[5]),
                                        "popped": int(work[0]), "relaxed": int(work[1]),
                                        "query_reads": int(work[2])})
 
@@ -151,6 +153,11 @@ class Oracle:
             return self._export(h)
         finally:
             self.L.orc_free(h)
+
+    def set_time_cap(self, seconds: float) -> None:
+        """Caps later builds' generation (reference schedule) at `seconds`
+        (0 = none): hubs not started by then are not searched."""
+        self.L.orc_set_time_cap(float(seconds))
 
     def clean(self, labels: Labels, K: int, threads: int = 1, mode: int = 0) -> Labels:
         """hop_constrained_clean_L on an arbitrary sorted label set."""

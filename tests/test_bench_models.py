@@ -36,3 +36,24 @@ def test_captured_traffic_is_read_from_the_committed_profile():
     assert v["capture"].startswith("profiles/") and isinstance(v["current"], bool)
     args.n = 200_000
     assert bench.captured_traffic(args) is None
+
+
+def test_reference_arm_runs_without_the_product_library():
+    """bench.py --impl reference builds the index with the oracle on the CPU
+    (the same seeded graph, generated by the oracle library) and never maps
+    libhsdl.so; a time cap turns the build into a watchdog-capped sample."""
+    import subprocess
+    import sys
+
+    code = ("import sys, json, argparse; sys.path.insert(0, %r); import bench; "
+            "a = argparse.Namespace(n=3000, K=5, queries=20000, steps=1, warmup=1, ref_build_cap=0.0); "
+            "r = bench.run_reference(a, None, 0, 1, 0); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(json.dumps({'hsdl': 'libhsdl.so' in maps, 'oracle': 'liboracle.so' in maps, "
+            "'hubs': r['build']['hubs_searched'], 'capped': r['build']['capped'], 'v': r['value']}))") % bench.ROOT
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, check=True).stdout
+    import json
+
+    d = json.loads(out.strip().splitlines()[-1])
+    assert d["oracle"] and not d["hsdl"]
+    assert d["hubs"] == 3000 and not d["capped"] and d["v"] > 0
