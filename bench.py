@@ -64,9 +64,10 @@ def parse():
     ap.add_argument("--plain-unbatched-rates", default="1e4,3e4,1e5",
                     help="offered rates of the plain path with one hsdl_query_batch call per request")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path sweep")
-    ap.add_argument("--ref-build-cap", type=float, default=300.0,
+    ap.add_argument("--ref-build-cap", type=float, default=600.0,
                     help="--impl reference: cap (s) on the CPU generation (0 = none); the full 1M-vertex build "
-                         "takes about 11 min on 16 Grace cores, so by default the build is a capped sample")
+                         "took 419 s (generation 356 s) on the 16 Grace cores of a GB300 host, so the default cap only "
+                         "guards a slower host")
     ap.add_argument("--workload", choices=["plain", "batched", "stress", "serving-mix"], default="plain",
                     help="batched: many small graphs built together; stress: the 4M-vertex graph with Zipf "
                          "queries; serving-mix: 65 resident graphs, Poisson queries over all of them while new "
