@@ -211,8 +211,9 @@ def algorithmic_bytes(off: np.ndarray, s, t, k, per_label: int = 12) -> int:
     """Per query: per_label bytes for every label of both rows (the join must
     read every one) and 32 B for the two offset pairs - the per-query figure
     12 (|L_s| + |L_t|) + 32 of the hot-path scope, which counts a label as its
-    (hub, hop, distance) triple.  The index stores 8 bytes per label (hub:32 |
-    hop:4 | distance:28); per_label = 8 gives that count."""
+    (hub, hop, distance) triple.  The joins stream the index's stored keys, 4
+    or 8 bytes per label (hsdl_index_info.query_key_bytes); per_label = that
+    width gives the bytes they must move."""
     ln = np.diff(off)
     rows = ln[s].astype(np.int64) + ln[t].astype(np.int64)
     rows[s == t] = 0
@@ -547,14 +548,16 @@ def run_ours(args, dist, rank, world, local):
         cap = captured_traffic(args)
         launch_s = kernel_ms / 1000.0 / args.steps
         achieved = bytes_per_launch / launch_s / 1e9
-        packed = algorithmic_bytes(off, s, t, k, per_label=8)
+        key_bytes = int(info.get("query_key_bytes", 8))  # bytes per label the join streams (4 or 8)
+        packed = algorithmic_bytes(off, s, t, k, per_label=key_bytes)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": (cap["bytes"] if cap and cap["current"] else None), "traffic_capture": cap,
                 "kernel": "k_query", "algorithmic_bytes_per_launch": bytes_per_launch,
                 "bytes_per_query": round(bytes_per_launch / args.queries, 1),
                 "byte_model": "12 B per label of both rows + 32 B of row offsets per query",
-                "stored_key_bytes": {"per_launch": packed, "achieved": round(packed / launch_s / 1e9, 1),
+                "stored_key_bytes": {"per_launch": packed, "bytes_per_label": key_bytes,
+                                     "achieved": round(packed / launch_s / 1e9, 1),
                                      "frac": round(packed / launch_s / 1e9 / peak, 4)}}
         cpu = None
         if not args.no_cpu_baseline:
