@@ -44,6 +44,15 @@ namespace hsdl {
 
 namespace {
 
+// Blocks of 256 threads per SM the loop runs with by default (its registers
+// are capped so that they fit at once).  At n = 1M, 2 / 3 / 4 blocks per SM
+// saturated at 147 / 205 / 279 M q/s; 6 blocks (which fit once the requests
+// moved to shared memory: 40 registers) saturated lower, at 263 M q/s, with
+// p99 1.9 ms already at 100 M/s offered: the workers' shares of the tickets
+// shrink with their number, so each answers smaller batches, and more warps
+// poll the one mirrored tail.
+constexpr int kServeBlocksPerSm = 4;
+
 struct IndexDesc {
   const int64_t* off;
   const uint64_t* key;
@@ -121,11 +130,24 @@ __device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
 // coalesced store.  A worker answers all of its published tickets (up to 32
 // at once: their requests are read in parallel and their rows prefetched),
 // one after another.
+// One request of a worker's batch, kept in shared memory while the batch is
+// answered (in registers, the 32 lanes' requests and index descriptors took
+// the loop to 64 registers; from shared memory the join keeps its own).
+struct ReqSlot {
+  const int64_t* off;
+  const void* key;  // 4-byte keys (Fmt32) when is32, else 8-byte keys
+  int32_t s, t, k, n;
+  uint32_t fmt;     // hub_shift | dist_bits << 8 of the 4-byte keys
+  int32_t valid;
+  int32_t is32;
+  int32_t pad;
+};
+
 template <int G>
-__global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
-                                               unsigned long long* comp, unsigned long long mask,
-                                               const IndexDesc* descs, int32_t max_idx, long long idle_ns,
-                                               unsigned long long base) {
+__global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
+                                                                 unsigned long long* comp, unsigned long long mask,
+                                                                 const IndexDesc* descs, int32_t max_idx,
+                                                                 long long idle_ns, unsigned long long base) {
   constexpr int Q = 32 / G;  // requests answered at once by one warp
   const int lane = lane_id();
   const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -151,6 +173,8 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
       __nanosleep(100);
     }
   }
+  __shared__ ReqSlot s_req[256 / 32][32];
+  ReqSlot* req = s_req[threadIdx.x >> 5];
   const unsigned long long W = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
   const unsigned long long w = (unsigned long long)(gw - 1);
   const int grp = lane / G;
@@ -167,61 +191,61 @@ __global__ void __launch_bounds__(256) k_serve(DevCtl* ctl, const HostCtl* hctl,
     if (avail) {
       backoff = 64;
       const int cnt = __popc(avail);
-      int4 r = make_int4(-1, 0, 0, 0);
-      if (lane < cnt) r = ld_volatile_v4(ring + (mine_tk & mask));
-      // every lane looks up its own request's index (and prefetches its rows
-      // into L2 when the warp has several to answer)
-      IndexDesc d{nullptr, nullptr, nullptr, 0, 0, 0, 0};
-      if (lane < cnt && r.x >= 0 && r.x < max_idx) {
-        d.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
-        d.key = (const uint64_t*)__ldcg((const unsigned long long*)&descs[r.x].key);
-        d.key32 = (const uint32_t*)__ldcg((const unsigned long long*)&descs[r.x].key32);
-        d.n = __ldcg(&descs[r.x].n);
-        d.valid = __ldcg(&descs[r.x].valid);
-        d.fmt = __ldcg(&descs[r.x].fmt);
-        if (d.valid && cnt > Q) {
-          if (d.key32) prefetch_rows(d.off, d.key32, d.n, r.y, r.z);
-          else prefetch_rows(d.off, d.key, d.n, r.y, r.z);
+      // every lane reads its own request and looks up its index (and
+      // prefetches its rows into L2 when the warp has several to answer)
+      if (lane < cnt) {
+        const int4 r = ld_volatile_v4(ring + (mine_tk & mask));
+        ReqSlot q{nullptr, nullptr, r.y, r.z, r.w, 0, 0u, 0, 0, 0};
+        if (r.x >= 0 && r.x < max_idx) {
+          q.valid = __ldcg(&descs[r.x].valid);
+          q.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
+          const void* k32 = (const void*)__ldcg((const unsigned long long*)&descs[r.x].key32);
+          q.is32 = k32 != nullptr;
+          q.key = k32 ? k32 : (const void*)__ldcg((const unsigned long long*)&descs[r.x].key);
+          q.n = __ldcg(&descs[r.x].n);
+          q.fmt = __ldcg(&descs[r.x].fmt);
+          if (q.valid && cnt > Q) {
+            if (q.is32) prefetch_rows(q.off, (const uint32_t*)q.key, q.n, r.y, r.z);
+            else prefetch_rows(q.off, (const uint64_t*)q.key, q.n, r.y, r.z);
+          }
         }
+        if (!q.valid) atomicAdd(&ctl->bad, 1ull);
+        req[lane] = q;
       }
-      if (lane < cnt && !d.valid) atomicAdd(&ctl->bad, 1ull);
+      __syncwarp();
       int32_t mine = INT_MAX;
       for (int r0 = 0; r0 < cnt; r0 += Q) {
-        // group grp answers request j = r0 + grp, held by lane j
-        const int j = min(r0 + grp, 31);
-        const int jvalid = __shfl_sync(0xffffffffu, d.valid, j);  // every lane shuffles
-        const bool active = r0 + grp < cnt && jvalid != 0;
-        const int s = __shfl_sync(0xffffffffu, r.y, j);
-        const int t = __shfl_sync(0xffffffffu, r.z, j);
-        const int k = __shfl_sync(0xffffffffu, r.w, j);
-        const int64_t* off = (const int64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.off, j);
-        const uint64_t* kr = (const uint64_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.key, j);
-        const uint32_t* k32 = (const uint32_t*)__shfl_sync(0xffffffffu, (unsigned long long)d.key32, j);
-        const uint32_t fmt = __shfl_sync(0xffffffffu, d.fmt, j);
-        const int n = __shfl_sync(0xffffffffu, d.n, j);
+        // group grp answers request r0 + grp (the lanes of a group read the
+        // same slot: one shared-memory broadcast)
+        const ReqSlot& q = req[min(r0 + grp, 31)];
+        const bool active = r0 + grp < cnt && q.valid != 0;
         // groups of one warp may serve indexes of both key formats: each
         // format's join runs, warp-wide, only if some group needs it
-        const bool is32 = k32 != nullptr;
-        const unsigned m32 = __ballot_sync(0xffffffffu, active && is32);
-        const unsigned m64 = __ballot_sync(0xffffffffu, active && !is32);
+        const unsigned m32 = __ballot_sync(0xffffffffu, active && q.is32);
+        const unsigned m64 = __ballot_sync(0xffffffffu, active && !q.is32);
         int32_t ans = INT_MAX;
         if (m32) {
-          const int32_t a = group_query<G>(active && is32, n, off, k32, s, t, k, Fmt32{fmt & 0xFFu, fmt >> 8});
-          if (is32) ans = a;
+          const int32_t a = group_query<G>(active && q.is32, q.n, q.off, (const uint32_t*)q.key, q.s, q.t, q.k,
+                                           Fmt32{q.fmt & 0xFFu, q.fmt >> 8});
+          if (q.is32) ans = a;
         }
         if (m64) {
-          const int32_t a = group_query<G>(active && !is32, n, off, kr, s, t, k, Fmt64{});
-          if (!is32) ans = a;
+          const int32_t a = group_query<G>(active && !q.is32, q.n, q.off, (const uint64_t*)q.key, q.s, q.t, q.k,
+                                           Fmt64{});
+          if (!q.is32) ans = a;
         }
         // lane j takes the answer of the group that served it
         const int src = (lane >= r0 && lane < r0 + Q) ? (lane - r0) * G : 0;
         const int32_t got = __shfl_sync(0xffffffffu, ans, src);
         if (lane >= r0 && lane < r0 + Q) mine = got;
       }
+      __syncwarp();
       // one 8-byte store per answer carries its ticket, so the host needs no
       // ordering between slots
-      if (lane < cnt)
-        st_relaxed_sys(comp + (mine_tk & mask), ((unsigned long long)(uint32_t)(mine_tk + 1) << 32) | (uint32_t)mine);
+      if (lane < cnt) {
+        const unsigned long long tk = base + 8ull * (w + (kk >> 3) * W) + (kk & 7ull);
+        st_relaxed_sys(comp + (tk & mask), ((unsigned long long)(uint32_t)(tk + 1) << 32) | (uint32_t)mine);
+      }
       if (lane == 0) atomicAdd(&ctl->processed, (unsigned long long)cnt);
       done += (unsigned long long)cnt;
       continue;
@@ -515,10 +539,8 @@ int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
                        : o.lanes_per_query == 16 ? resident_blocks(k_serve<16>, 256)
                                                  : resident_blocks(k_serve<32>, 256);
     const int most = S->sms * per_sm;
-    // default 4 per SM: at n = 1M, 2 / 3 / 4 / 5 blocks of 256 threads per SM
-    // saturated at 147 / 205 / 241 / 253 M q/s, and 4 still held p99 under
-    // 1 ms at 200 M q/s offered (5 raised latency at every load)
-    if (S->opts.ctas <= 0) S->opts.ctas = std::min(most, S->sms * 4);
+    // default: as many as fit (kServeBlocksPerSm per SM)
+    if (S->opts.ctas <= 0) S->opts.ctas = std::min(most, S->sms * kServeBlocksPerSm);
     if (S->opts.ctas > most) {
       delete S;
       set_error("ctas must be at most " + std::to_string(most) + " (blocks of the loop that fit on the GPU at once)");
