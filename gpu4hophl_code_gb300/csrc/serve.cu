@@ -44,14 +44,14 @@ namespace hsdl {
 
 namespace {
 
-// Blocks of 256 threads per SM the loop runs with by default (its registers
-// are capped so that they fit at once).  At n = 1M, 2 / 3 / 4 blocks per SM
-// saturated at 147 / 205 / 279 M q/s; 6 blocks (which fit once the requests
-// moved to shared memory: 40 registers) saturated lower, at 263 M q/s, with
-// p99 1.9 ms already at 100 M/s offered: the workers' shares of the tickets
-// shrink with their number, so each answers smaller batches, and more warps
-// poll the one mirrored tail.
-constexpr int kServeBlocksPerSm = 4;
+// Blocks of 256 threads per SM the loop's registers are capped for (40
+// registers: its requests wait in shared memory), and the number it runs with
+// by default.  At n = 1M, 2 / 3 / 4 blocks per SM saturated at 147 / 205 /
+// 282 M q/s; 6 blocks saturated lower (266 M q/s) with a higher p99 at every
+// load: the workers' shares of the tickets shrink with their number, so each
+// answers smaller batches.
+constexpr int kServeBlocksPerSm = 6;
+constexpr int kServeDefaultBlocksPerSm = 4;
 
 struct IndexDesc {
   const int64_t* off;
@@ -67,6 +67,14 @@ struct ServeReq {
   int32_t g, s, t, k;
 };
 
+// Copies of the mirrored tail, each on its own 128-byte line: the workers of
+// block b poll copy b mod kTailCopies, so thousands of idle warps do not all
+// poll one L2 line.  With one copy, p99 at n = 1M was 425 us at 100 M/s
+// offered and 294 us at 200 M/s (at moderate load most workers are idle and
+// polling); with 64, 188 and 210 us, and 318 against 426 us at 260 M/s.
+constexpr int kTailCopies = 64;  // written two per lane by the dispatcher warp
+constexpr int kTailStride = 16;  // u64 per 128-byte line
+
 struct DevCtl {
   unsigned long long head;       // next ticket to claim
   unsigned long long processed;  // tickets answered
@@ -74,6 +82,8 @@ struct DevCtl {
   unsigned int exit_reason;      // 1 idle, 2 stop
   unsigned int pad;
   unsigned long long dev_tail;   // device-side mirror of the host's tail
+  unsigned long long pad2[11];
+  unsigned long long tail_copy[kTailCopies * kTailStride];  // the mirror, fanned out
 };
 
 struct HostCtl {
@@ -114,6 +124,10 @@ __device__ inline unsigned long long ld_acquire_gpu(const unsigned long long* p)
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ inline void st_relaxed_gpu(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ inline void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ inline void st_release_gpu(unsigned long long* p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -152,22 +166,44 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
   const int lane = lane_id();
   const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (gw == 0) {
-    if (lane != 0) return;
-    unsigned long long last = ld_acquire_gpu(&ctl->dev_tail);
-    long long idle_start = globaltimer_ns();
+    // the dispatcher warp: lane 0 polls the host; on a new tail every lane
+    // writes two of the tail's copies
+    unsigned long long last = 0;
+    if (lane == 0) last = ld_acquire_gpu(&ctl->dev_tail);
+    last = __shfl_sync(0xffffffffu, last, 0);
+    long long idle_start = 0;
+    if (lane == 0) idle_start = globaltimer_ns();
     for (;;) {
-      const unsigned long long t = ld_acquire_sys(&hctl->tail);
-      if (t != last) {
-        st_release_gpu(&ctl->dev_tail, t);
-        last = t;
-        idle_start = globaltimer_ns();
+      unsigned long long t = 0;
+      unsigned int stop = 0;
+      if (lane == 0) {
+        t = ld_acquire_sys(&hctl->tail);
+        stop = ld_volatile_u32(&hctl->stop);
       }
-      if (ld_volatile_u32(&hctl->stop)) {
-        atomicMax(&ctl->exit_reason, 2u);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      stop = __shfl_sync(0xffffffffu, stop, 0);
+      if (t != last) {
+        // the warp barrier orders lane 0's acquire before every lane's fence,
+        // and each fence makes its lane's relaxed stores release the tail
+        // (and the ring entries the acquire made visible) to the workers
+        __syncwarp();
+        fence_acq_rel_gpu();
+        for (int c = lane; c < kTailCopies; c += 32) st_relaxed_gpu(&ctl->tail_copy[c * kTailStride], t);
+        if (lane == 0) {
+          st_release_gpu(&ctl->dev_tail, t);
+          idle_start = globaltimer_ns();
+        }
+        last = t;
+      }
+      if (stop) {
+        if (lane == 0) atomicMax(&ctl->exit_reason, 2u);
         return;
       }
-      if (globaltimer_ns() - idle_start > idle_ns && *(volatile unsigned long long*)&ctl->processed >= last) {
-        atomicMax(&ctl->exit_reason, 1u);
+      int idle = 0;
+      if (lane == 0)
+        idle = globaltimer_ns() - idle_start > idle_ns && *(volatile unsigned long long*)&ctl->processed >= last;
+      if (__shfl_sync(0xffffffffu, idle, 0)) {
+        if (lane == 0) atomicMax(&ctl->exit_reason, 1u);
         return;
       }
       __nanosleep(100);
@@ -182,7 +218,7 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
   unsigned int backoff = 64;
   for (;;) {
     unsigned long long tail = 0;
-    if (lane == 0) tail = ld_acquire_gpu(&ctl->dev_tail);
+    if (lane == 0) tail = ld_acquire_gpu(&ctl->tail_copy[(blockIdx.x % kTailCopies) * kTailStride]);
     tail = __shfl_sync(0xffffffffu, tail, 0);
     // this worker's (done + lane)-th ticket
     const unsigned long long kk = done + (unsigned long long)lane;
@@ -539,8 +575,7 @@ int hsdl_serve_create(const hsdl_serve_opts* opts, hsdl_server** out) {
                        : o.lanes_per_query == 16 ? resident_blocks(k_serve<16>, 256)
                                                  : resident_blocks(k_serve<32>, 256);
     const int most = S->sms * per_sm;
-    // default: as many as fit (kServeBlocksPerSm per SM)
-    if (S->opts.ctas <= 0) S->opts.ctas = std::min(most, S->sms * kServeBlocksPerSm);
+    if (S->opts.ctas <= 0) S->opts.ctas = std::min(most, S->sms * kServeDefaultBlocksPerSm);
     if (S->opts.ctas > most) {
       delete S;
       set_error("ctas must be at most " + std::to_string(most) + " (blocks of the loop that fit on the GPU at once)");
