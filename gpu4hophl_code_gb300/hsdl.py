@@ -599,7 +599,9 @@ class Server:
         s = np.ascontiguousarray(s, np.int32)
         t = np.ascontiguousarray(t, np.int32)
         k = np.ascontiguousarray(k, np.int32)
-        ans = np.zeros(len(s), np.int32) if want_answers else None
+        # written (not just allocated) before the run: first touches of fresh
+        # pages inside the timed run would stall the consumer threads
+        ans = np.full(len(s), -1, np.int32) if want_answers else None
         o = N.hsdl_loadgen_opts()
         o.struct_size = C.sizeof(N.hsdl_loadgen_opts)
         o.n = len(s)
