@@ -44,14 +44,15 @@ namespace hsdl {
 
 namespace {
 
-// Blocks of 256 threads per SM the loop's registers are capped for (40
-// registers: its requests wait in shared memory), and the number it runs with
-// by default.  At n = 1M, 2 / 3 / 4 blocks per SM saturated at 147 / 205 /
-// 282 M q/s; 6 blocks saturated lower (266 M q/s) with a higher p99 at every
-// load: the workers' shares of the tickets shrink with their number, so each
-// answers smaller batches.
+// Blocks of 256 threads per SM the loop is compiled for (40 registers) and
+// runs with by default.  At n = 1M: 2 / 3 / 4 blocks per SM saturated at 147
+// / 205 / 275-283 M q/s; 6 blocks at 315 M q/s, holding p99 at 314 us at
+// 290 M/s offered (4 blocks: 3.2 ms).  Six blocks scale only because a
+// request waits in 16 bytes of shared memory: with 48-byte slots the blocks'
+// shared memory cost the SMs the L1 that holds the joins' rows, and 6 blocks
+// saturated lower than 4 (266 M q/s).
 constexpr int kServeBlocksPerSm = 6;
-constexpr int kServeDefaultBlocksPerSm = 4;
+constexpr int kServeDefaultBlocksPerSm = 6;
 
 struct IndexDesc {
   const int64_t* off;
@@ -144,18 +145,12 @@ __device__ inline unsigned int ld_volatile_dev_u32(const unsigned int* p) {
 // coalesced store.  A worker answers all of its published tickets (up to 32
 // at once: their requests are read in parallel and their rows prefetched),
 // one after another.
-// One request of a worker's batch, kept in shared memory while the batch is
-// answered (in registers, the 32 lanes' requests and index descriptors took
-// the loop to 64 registers; from shared memory the join keeps its own).
-struct ReqSlot {
-  const int64_t* off;
-  const void* key;  // 4-byte keys (Fmt32) when is32, else 8-byte keys
-  int32_t s, t, k, n;
-  uint32_t fmt;     // hub_shift | dist_bits << 8 of the 4-byte keys
-  int32_t valid;
-  int32_t is32;
-  int32_t pad;
-};
+// A worker's batch of requests waits in shared memory while it is answered
+// (in registers, the 32 lanes' requests and index descriptors took the loop
+// to 64 registers), one int4 per request: graph id (-1 when it names no
+// resident index), s, t, k.  Only 16 bytes a request: the shared memory the
+// blocks take comes out of the SMs' L1, which holds the rows the joins read
+// (48-byte slots with the descriptors cost 6 blocks per SM a 100 KB carveout).
 
 template <int G>
 __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, const HostCtl* hctl, const int4* ring,
@@ -209,8 +204,8 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
       __nanosleep(100);
     }
   }
-  __shared__ ReqSlot s_req[256 / 32][32];
-  ReqSlot* req = s_req[threadIdx.x >> 5];
+  __shared__ int4 s_req[256 / 32][32];
+  int4* req = s_req[threadIdx.x >> 5];
   const unsigned long long W = (((unsigned long long)gridDim.x * blockDim.x) >> 5) - 1;
   const unsigned long long w = (unsigned long long)(gw - 1);
   const int grp = lane / G;
@@ -227,48 +222,46 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
     if (avail) {
       backoff = 64;
       const int cnt = __popc(avail);
-      // every lane reads its own request and looks up its index (and
-      // prefetches its rows into L2 when the warp has several to answer)
+      // every lane reads its own request and checks its index.  (An L2 bulk
+      // prefetch of the batch's rows here measured p99 410 against 297 us at
+      // 260 M/s offered, n = 1M: the rows of up to 32 requests, joined one
+      // after another, were partly evicted before use.)
       if (lane < cnt) {
-        const int4 r = ld_volatile_v4(ring + (mine_tk & mask));
-        ReqSlot q{nullptr, nullptr, r.y, r.z, r.w, 0, 0u, 0, 0, 0};
-        if (r.x >= 0 && r.x < max_idx) {
-          q.valid = __ldcg(&descs[r.x].valid);
-          q.off = (const int64_t*)__ldcg((const unsigned long long*)&descs[r.x].off);
-          const void* k32 = (const void*)__ldcg((const unsigned long long*)&descs[r.x].key32);
-          q.is32 = k32 != nullptr;
-          q.key = k32 ? k32 : (const void*)__ldcg((const unsigned long long*)&descs[r.x].key);
-          q.n = __ldcg(&descs[r.x].n);
-          q.fmt = __ldcg(&descs[r.x].fmt);
-          if (q.valid && cnt > Q) {
-            if (q.is32) prefetch_rows(q.off, (const uint32_t*)q.key, q.n, r.y, r.z);
-            else prefetch_rows(q.off, (const uint64_t*)q.key, q.n, r.y, r.z);
-          }
+        int4 r = ld_volatile_v4(ring + (mine_tk & mask));
+        const bool valid = r.x >= 0 && r.x < max_idx && __ldcg(&descs[r.x].valid) != 0;
+        if (!valid) {
+          atomicAdd(&ctl->bad, 1ull);
+          r.x = -1;
         }
-        if (!q.valid) atomicAdd(&ctl->bad, 1ull);
-        req[lane] = q;
+        req[lane] = r;
       }
       __syncwarp();
       int32_t mine = INT_MAX;
       for (int r0 = 0; r0 < cnt; r0 += Q) {
         // group grp answers request r0 + grp (the lanes of a group read the
-        // same slot: one shared-memory broadcast)
-        const ReqSlot& q = req[min(r0 + grp, 31)];
-        const bool active = r0 + grp < cnt && q.valid != 0;
+        // same slot and descriptor: broadcasts)
+        const int4 q = req[min(r0 + grp, 31)];
+        const bool active = r0 + grp < cnt && q.x >= 0;
+        const IndexDesc* dp = descs + (active ? q.x : 0);
+        const int64_t* off = (const int64_t*)__ldcg((const unsigned long long*)&dp->off);
+        const void* k32 = (const void*)__ldcg((const unsigned long long*)&dp->key32);
+        const bool is32 = k32 != nullptr;
         // groups of one warp may serve indexes of both key formats: each
         // format's join runs, warp-wide, only if some group needs it
-        const unsigned m32 = __ballot_sync(0xffffffffu, active && q.is32);
-        const unsigned m64 = __ballot_sync(0xffffffffu, active && !q.is32);
+        const unsigned m32 = __ballot_sync(0xffffffffu, active && is32);
+        const unsigned m64 = __ballot_sync(0xffffffffu, active && !is32);
+        const int n = __ldcg(&dp->n);
         int32_t ans = INT_MAX;
         if (m32) {
-          const int32_t a = group_query<G>(active && q.is32, q.n, q.off, (const uint32_t*)q.key, q.s, q.t, q.k,
-                                           Fmt32{q.fmt & 0xFFu, q.fmt >> 8});
-          if (q.is32) ans = a;
+          const uint32_t fmt = __ldcg(&dp->fmt);
+          const int32_t a = group_query<G>(active && is32, n, off, (const uint32_t*)k32, q.y, q.z, q.w,
+                                           Fmt32{fmt & 0xFFu, fmt >> 8});
+          if (is32) ans = a;
         }
         if (m64) {
-          const int32_t a = group_query<G>(active && !q.is32, q.n, q.off, (const uint64_t*)q.key, q.s, q.t, q.k,
-                                           Fmt64{});
-          if (!q.is32) ans = a;
+          const uint64_t* k64 = (const uint64_t*)__ldcg((const unsigned long long*)&dp->key);
+          const int32_t a = group_query<G>(active && !is32, n, off, k64, q.y, q.z, q.w, Fmt64{});
+          if (!is32) ans = a;
         }
         // lane j takes the answer of the group that served it
         const int src = (lane >= r0 && lane < r0 + Q) ? (lane - r0) * G : 0;
@@ -836,6 +829,12 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
     __atomic_store_n(&S->hctl->stop, 0u, __ATOMIC_RELEASE);
   }
   HSDL_TRY(launch_if_needed(S));
+  // The requests as the ring holds them, packed before the run: a client hands
+  // the server whole requests, and gathering them from four arrays inside the
+  // run made the one producer thread the ceiling (the loop then saturated near
+  // 280 M requests/s whatever the GPU could do).
+  std::vector<int4> packed((size_t)n);
+  for (int64_t i = 0; i < n; i++) packed[i] = make_int4(o->g[i], o->s[i], o->t[i], o->k[i]);
   int64_t t_start = mono_ns() + 2000000;  // 2 ms to let the threads start
   std::thread producer([&] {
     int64_t i = 0;
@@ -844,12 +843,13 @@ int hsdl_serve_loadgen(hsdl_server* S, const hsdl_loadgen_opts* o, hsdl_loadgen_
       if (now < arrive[i]) continue;
       uint64_t room = S->cap - (S->tail - min_consumed());
       if (room == 0) continue;
-      int64_t j = i;
-      while (j < n && (uint64_t)(j - i) < room && arrive[j] <= now && j - i < 4096) {
-        uint64_t tk = S->tail + (j - i);
-        S->ring[tk & S->mask] = make_int4(o->g[j], o->s[j], o->t[j], o->k[j]);
-        j++;
-      }
+      // every request that has arrived, within the room left and 4,096 at a time
+      const int64_t lim = std::min<int64_t>(n, i + (int64_t)std::min<uint64_t>(room, 4096));
+      const int64_t j = std::upper_bound(arrive.begin() + i, arrive.begin() + lim, now) - arrive.begin();
+      const uint64_t pos = S->tail & S->mask;
+      const int64_t first = std::min<int64_t>(j - i, (int64_t)(S->cap - pos));
+      std::memcpy(S->ring + pos, packed.data() + i, sizeof(int4) * (size_t)first);
+      if (j - i > first) std::memcpy(S->ring, packed.data() + i + first, sizeof(int4) * (size_t)(j - i - first));
       S->tail += (uint64_t)(j - i);
       __atomic_store_n(&S->hctl->tail, (unsigned long long)S->tail, __ATOMIC_RELEASE);
       i = j;
