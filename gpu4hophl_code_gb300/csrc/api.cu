@@ -775,6 +775,7 @@ int hsdl_set_query_tuning(hsdl_index* idx, const hsdl_query_tuning* t) {
   idx->q_threads = t->block_threads;
   idx->q_ahead = t->prefetch_ahead;
   idx->q_lanes = t->lanes_per_query;
+  idx->q_tuned = true;
   return HSDL_OK;
 }
 

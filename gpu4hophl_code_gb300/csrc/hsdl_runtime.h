@@ -113,6 +113,7 @@ struct hsdl_index_impl {
   int32_t q_threads = 512;    // query kernel: threads per block
   int32_t q_lanes = 32;       // query kernel: lanes per query (8, 16 or 32)
   int32_t q_ahead = 0;        // query kernel: queries prefetched ahead per warp (0 = none)
+  bool q_tuned = false;       // set by hsdl_set_query_tuning: the defaults below no longer apply
   int64_t total = 0;
   int64_t before = 0, after = 0, max_row = 0;
   int32_t waves = 0;

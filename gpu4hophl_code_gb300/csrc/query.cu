@@ -141,6 +141,10 @@ int preload_query_kernels() {
 int make_query_keys(hsdl_index_impl* idx) {
   cudaStream_t st = idx->stream;
   idx->key32.release();
+  if (!idx->q_tuned) {  // the 8-byte join's default shape
+    idx->q_threads = 512;
+    idx->q_ahead = 0;
+  }
   const int H = bits_for((uint32_t)std::max(0, idx->n - 1)), P = bits_for((uint32_t)idx->K);
   const int D = 32 - H - P;
   if (D < 1 || idx->total <= 0) return HSDL_OK;
@@ -155,6 +159,15 @@ int make_query_keys(hsdl_index_impl* idx) {
   HSDL_CUDA(cudaStreamSynchronize(st));
   mx.release();
   if (D < 32 && (maxd >> D) != 0) return HSDL_OK;
+  // default launch shape of the join over 4-byte keys: 1,024 threads per block
+  // and an L2 prefetch of the rows one query ahead (the prefetching variant
+  // compiles to 32 registers, so two such blocks fill an SM's 64 warps): at
+  // n = 1M 404 M q/s, against 391 M for 512 threads without prefetch (38
+  // registers, 48 warps) and 384 M for 512 threads with it
+  if (!idx->q_tuned) {
+    idx->q_threads = 1024;
+    idx->q_ahead = 1;
+  }
   Fmt32 f{(uint32_t)(P + D), (uint32_t)D};
   HSDL_TRY(idx->key32.alloc(idx->total + kRowPad, st));
   HSDL_CUDA(cudaMemsetAsync(idx->key32.p + idx->total, 0xFF, sizeof(uint32_t) * kRowPad, st));
