@@ -31,10 +31,15 @@ namespace {
 // plain kernel carries no prefetch code at all).
 // (Capping it at 32 registers for 64 resident warps per SM, against 38 and 48
 // warps, cut the rate from 322 M to 221 M q/s at n = 1M.)
+// Over 4-byte keys the kernel is held to 32 registers (two blocks of 1,024
+// threads, 64 warps per SM; it compiles without spills): at n = 1M 426 M q/s
+// against 391 M at 38 registers (48 warps).  Over 8-byte keys the same cap
+// spills and cost a third of the rate, so that join keeps its registers.
 template <int G, bool PF, class KT, class F>
-__global__ void k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
-                        const int32_t* __restrict__ qk, const int64_t* __restrict__ off,
-                        const KT* __restrict__ key, int32_t* __restrict__ out, int ahead, F f) {
+__global__ void __launch_bounds__(1024, sizeof(KT) == 4 ? 2 : 1)
+    k_query(int32_t n, int64_t nq, const int32_t* __restrict__ qs, const int32_t* __restrict__ qt,
+            const int32_t* __restrict__ qk, const int64_t* __restrict__ off, const KT* __restrict__ key,
+            int32_t* __restrict__ out, int ahead, F f) {
   constexpr int Q = 32 / G;  // queries per warp step
   const int lane = lane_id(), grp = lane / G, gl = lane & (G - 1);
   const int64_t step = (((int64_t)gridDim.x * blockDim.x) >> 5) * Q;
@@ -160,13 +165,13 @@ int make_query_keys(hsdl_index_impl* idx) {
   mx.release();
   if (D < 32 && (maxd >> D) != 0) return HSDL_OK;
   // default launch shape of the join over 4-byte keys: 1,024 threads per block
-  // and an L2 prefetch of the rows one query ahead (the prefetching variant
-  // compiles to 32 registers, so two such blocks fill an SM's 64 warps): at
-  // n = 1M 404 M q/s, against 391 M for 512 threads without prefetch (38
-  // registers, 48 warps) and 384 M for 512 threads with it
+  // (two blocks fill an SM's 64 warps at its 32 registers), no prefetch: at
+  // n = 1M 426 M q/s, against 405 M for 512 threads and 406 M for 1,024 with
+  // an L2 prefetch of the rows one query ahead (which also read 1.5x the
+  // DRAM bytes: prefetched rows were evicted before their join)
   if (!idx->q_tuned) {
     idx->q_threads = 1024;
-    idx->q_ahead = 1;
+    idx->q_ahead = 0;
   }
   Fmt32 f{(uint32_t)(P + D), (uint32_t)D};
   HSDL_TRY(idx->key32.alloc(idx->total + kRowPad, st));

@@ -304,7 +304,7 @@ def test_query_key_formats_agree_with_the_oracle(orc, wmax, key_bytes):
         assert info["query_key_hub_bits"] == 12
     # each join format's default launch shape
     tun = idx.query_tuning()
-    assert (tun["block_threads"], tun["prefetch_ahead"]) == ((1024, 1) if key_bytes == 4 else (512, 0))
+    assert (tun["block_threads"], tun["prefetch_ahead"]) == ((1024, 0) if key_bytes == 4 else (512, 0))
     ref = orc.build(g, K, threads=1)
     rng = np.random.default_rng(wmax)
     s = rng.integers(0, g.n, 200000).astype(np.int32)
