@@ -60,8 +60,13 @@ template <int G, bool PF, class KT, class F>
 int launch_query(hsdl_index_impl* idx, const KT* key, F f, int64_t nq, const int32_t* s, const int32_t* t,
                  const int32_t* k, int32_t* out, cudaStream_t st) {
   const int sms = device_sm_count();
-  const int threads = idx->q_threads;
   const int64_t warps = (nq + (32 / G) - 1) / (32 / G);
+  // a batch too small to give every SM a block runs in smaller blocks, so
+  // that it spreads over all SMs instead of crowding a few (a 1,024-thread
+  // block puts 32 of the batch's queries on one SM)
+  int threads = idx->q_threads;
+  if (warps * 32 < (int64_t)sms * threads)
+    threads = (int)std::max<int64_t>(64, std::min<int64_t>(threads, (warps * 32 / sms) & ~(int64_t)31));
   int64_t blocks = (warps * 32 + threads - 1) / threads;
   int64_t max_blocks = (int64_t)sms * resident_blocks(k_query<G, PF, KT, F>, threads);
   k_query<G, PF, KT, F><<<(unsigned)std::min(blocks, max_blocks), threads, 0, st>>>(idx->n, nq, s, t, k, idx->off.p,
