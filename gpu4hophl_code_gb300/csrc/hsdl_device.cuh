@@ -47,7 +47,8 @@ __host__ __device__ inline uint32_t lkey_hop(uint64_t k) { return hd_hop((uint32
 __host__ __device__ inline uint32_t lkey_dist(uint64_t k) { return hd_dist((uint32_t)k); }
 
 // Compact query key (4 B), used by the query joins when the index's ranges
-// fit: hub:H | hop:P | distance:D with H = bits of n - 1, P = bits of K and
+// fit: hub:H | hop:P | distance:D with H = bits of n (the all-ones key is
+// then a hub above every real one), P = bits of K and
 // D = 32 - H - P >= the bits of the largest distance in the index (n = 1M,
 // K = 5, weights <= 100: 20 | 3 | 9).  Unsigned order is again the label
 // order, so the rows keep their sort; a join streams half the bytes of the

@@ -155,7 +155,9 @@ int make_query_keys(hsdl_index_impl* idx) {
     idx->q_threads = 512;
     idx->q_ahead = 0;
   }
-  const int H = bits_for((uint32_t)std::max(0, idx->n - 1)), P = bits_for((uint32_t)idx->K);
+  // H holds 0..n, one more than the largest hub id, so an all-ones key reads
+  // as a hub above every real one (the join's end-of-row sentinel)
+  const int H = bits_for((uint32_t)std::max(0, idx->n)), P = bits_for((uint32_t)idx->K);
   const int D = 32 - H - P;
   if (D < 1 || idx->total <= 0) return HSDL_OK;
   const int sms = device_sm_count();

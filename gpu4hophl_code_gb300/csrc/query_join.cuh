@@ -27,36 +27,45 @@ namespace hsdl {
 // distance:28, format Fmt64) or uint32_t (the compact key, Fmt32) - so hop and
 // distance arrive with the hub id and a match needs no dependent load (a
 // layout with hub ids and hop|distance words in separate arrays measured
-// 238 M q/s against 322 M q/s for the 8-byte keys at n = 1M).
+// 238 M q/s against 322 M q/s for the 8-byte keys at n = 1M).  Distances are
+// below 2^28 in both formats, so a pair's sum fits int32.  At n = 1M (10M
+// queries, compact keys) the 32-bit minimum, the end-of-row sentinel below and
+// a two-step unroll took the join from 426 to 465 M q/s; carrying the hubs
+// instead of the keys (345), a one-key lookahead per row (463) and 16 or 8
+// lanes per query (275 / 170) did not help.
 template <int G, class KT, class F>
-__device__ inline long long lane_merge(const KT* A, int la, const KT* B, int lb, int k, int gl, F f) {
-  long long best = INT_MAX;
+__device__ inline int lane_merge(const KT* A, int la, const KT* B, int lb, int k, int gl, F f) {
+  int best = INT_MAX;
   const int tot = la + lb;
   const int d0 = (int)(((int64_t)tot * gl) / G), d1 = (int)(((int64_t)tot * (gl + 1)) / G);
   int lo = max(0, d0 - lb), hi = min(d0, la);
-  for (int span = la; span > 0; span >>= 1) {
-    if (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (f.hub(A[mid]) <= f.hub(B[d0 - 1 - mid])) lo = mid + 1; else hi = mid;
-    }
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (f.hub(A[mid]) <= f.hub(B[d0 - 1 - mid])) lo = mid + 1; else hi = mid;
   }
+  // An exhausted row reads as kEnd, whose hub field is above every real hub
+  // id (the compact key's H holds 0..n), so the other row's label goes first;
+  // inside the piece at most one row is exhausted (it ends by d1 <= la + lb),
+  // so equal hubs are always a common hub.
   constexpr KT kEnd = (KT)~(KT)0;
   int ia = lo, ib = d0 - lo;
   KT wa = ia < la ? A[ia] : kEnd;
   KT wb = ib < lb ? B[ib] : kEnd;
+#pragma unroll 2
   for (int step = d0; step < d1; step++) {
     const uint32_t ha = f.hub(wa), hb = f.hub(wb);
-    const bool take_a = ia < la && (ib >= lb || ha <= hb);
-    if (take_a && ha == hb) {  // a common hub: B's run of it starts at ib
+    const bool take_a = ha <= hb;  // A's label first on equal hubs
+    if (ha == hb) {                // a common hub: B's run of it starts at ib
       const int h1 = (int)f.hop(wa);
       if (h1 <= k) {
-        const long long da = f.dist(wa);
-        KT xb = wb;
-        for (int p = ib; p < lb; xb = (++p < lb) ? B[p] : (KT)0) {
-          if (f.hub(xb) != ha) break;
+        const int da = (int)f.dist(wa);
+        KT xb = wb;  // its hub is ha
+        for (int p = ib;;) {
           if (h1 + (int)f.hop(xb) > k) break;  // rows are hop-sorted within a hub
-          const long long c = da + f.dist(xb);
-          best = c < best ? c : best;
+          best = min(best, da + (int)f.dist(xb));
+          if (++p >= lb) break;
+          xb = B[p];
+          if (f.hub(xb) != ha) break;
         }
       }
     }
@@ -73,12 +82,9 @@ __device__ inline long long lane_merge(const KT* A, int la, const KT* B, int lb,
 
 // Min over the G lanes of each group (every lane of the warp must call it).
 template <int G>
-__device__ inline long long group_min(long long v) {
+__device__ inline int group_min(int v) {
 #pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    long long x = __shfl_xor_sync(0xffffffffu, v, o);
-    v = x < v ? x : v;
-  }
+  for (int o = G / 2; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -127,8 +133,6 @@ __device__ inline bool trivial_answer(int32_t n, int s, int t, int k, int32_t* a
   return false;
 }
 
-__device__ inline int32_t clamp_answer(long long best) { return best >= INT_MAX ? INT_MAX : (int32_t)best; }
-
 // Each group of G lanes answers its own (s, t, k), rows read from global
 // memory; every lane of the warp must call it (inactive groups pass
 // active = false).  Every lane of a group returns the group's answer.
@@ -136,7 +140,7 @@ template <int G, class KT, class F>
 __device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __restrict__ off,
                                       const KT* __restrict__ key, int s, int t, int k, F f) {
   int32_t ans = INT_MAX;
-  long long best = INT_MAX;
+  int best = INT_MAX;
   const bool trivial = !active || trivial_answer(n, s, t, k, &ans);
   if (!trivial) {
     int64_t a0 = off[s], a1 = off[s + 1], b0 = off[t], b1 = off[t + 1];
@@ -147,7 +151,7 @@ __device__ inline int32_t group_query(bool active, int32_t n, const int64_t* __r
     best = lane_merge<G>(key + a0, (int)(a1 - a0), key + b0, (int)(b1 - b0), k, lane_id() & (G - 1), f);
   }
   best = group_min<G>(best);
-  return trivial ? ans : clamp_answer(best);
+  return trivial ? ans : best;
 }
 
 template <int G>

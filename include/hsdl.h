@@ -300,7 +300,7 @@ typedef struct hsdl_index_info {
   int32_t build_wave_splits;     /* waves split in two because their candidates outgrew the memory left */
   int32_t build_pool_chunks;     /* device allocations the label pool grew by */
   int32_t query_key_bytes;       /* bytes per label the query joins stream: 4 when the index's ranges fit the
-                                    compact key hub:H | hop:P | distance:D (H = bits of n - 1, P = bits of K,
+                                    compact key hub:H | hop:P | distance:D (H = bits of n, P = bits of K,
                                     D = 32 - H - P), else 8 */
   int32_t query_key_hub_bits;    /* H of the compact key (0 with 8-byte keys) */
   int32_t build_pool_key_bytes;  /* bytes per label key in the generation's label pool (4 or 8) */

@@ -313,3 +313,26 @@ def test_query_key_formats_agree_with_the_oracle(orc, wmax, key_bytes):
     assert np.array_equal(idx.query(s, t, k), orc.query(ref, s, t, k))
     idx.close()
     dev.close()
+
+
+def test_compact_keys_at_a_power_of_two_vertex_count(orc):
+    """With n = 4,096 the compact key's hub field holds 0..n (13 bits), so the
+    all-ones end-of-row key reads as a hub above vertex 4,095, whose self
+    label ends its own row; queries on the last vertices answer as the
+    oracle's."""
+    g = H.HostGraph.erdos_renyi(4096, 16000, 1, 100, seed=67)
+    K = 4
+    dev, idx = gpu_build(g, K)
+    info = idx.info()
+    assert info["query_key_bytes"] == 4 and info["query_key_hub_bits"] == 13
+    ref = orc.build(g, K, threads=1)
+    rng = np.random.default_rng(67)
+    m = 100000
+    s = rng.integers(0, g.n, m).astype(np.int32)
+    t = rng.integers(0, g.n, m).astype(np.int32)
+    s[: m // 4] = g.n - 1 - rng.integers(0, 4, m // 4)
+    t[m // 4: m // 2] = g.n - 1
+    k = rng.integers(0, K + 1, m).astype(np.int32)
+    assert np.array_equal(idx.query(s, t, k), orc.query(ref, s, t, k))
+    idx.close()
+    dev.close()
