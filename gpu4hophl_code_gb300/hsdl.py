@@ -594,7 +594,7 @@ class Server:
         return out
 
     def loadgen(self, g, s, t, k, offered_qps: float = 0.0, seed: int = 1, want_answers: bool = True,
-                consumers: int = 8) -> dict:
+                consumers: int = 4) -> dict:
         g = np.ascontiguousarray(g, np.int32)
         s = np.ascontiguousarray(s, np.int32)
         t = np.ascontiguousarray(t, np.int32)
