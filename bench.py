@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--K", type=int, default=5)
     ap.add_argument("--cpu-baseline-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rates", default="5e6,2e7,5e7,1e8,1.5e8,2e8,2.3e8,2.6e8,2.75e8,2.9e8,3.2e8,3.5e8,0",
+    ap.add_argument("--serve-rates", default="5e6,2e7,5e7,1e8,1.5e8,2e8,2.3e8,2.6e8,2.75e8,2.825e8,2.9e8,3.05e8,3.2e8,3.5e8,0",
                     help="offered Poisson rates (q/s) for the serving loop and the plain path, run upwards until "
                          "the path saturates; 0 = as fast as the serving ring allows")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
