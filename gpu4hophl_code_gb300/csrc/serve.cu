@@ -226,8 +226,9 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
   const unsigned long long s0 = (unsigned long long)(first_gw - 1);         // the block's first slot
   const unsigned long long nb = (unsigned long long)((int)blockIdx.x * wpb + wpb - first_gw);  // its slots
   const int grp = lane / G;
-  unsigned long long t0 = 0;  // first ticket of the held chunk
-  int got = 8;                // tickets of it answered (8: none held)
+  unsigned long long t0 = 0;    // first ticket of the held chunk
+  int got = 8;                  // tickets of it answered (8: none held)
+  unsigned long long seen = 0;  // the latest tail this warp has acquired
   unsigned int backoff = 64;
   for (;;) {
     if (got == 8) {
@@ -237,10 +238,16 @@ __global__ void __launch_bounds__(256, kServeBlocksPerSm) k_serve(DevCtl* ctl, c
       t0 = base + 8ull * ((j / nb) * W + s0 + j % nb);
       got = 0;
     }
-    unsigned long long tail = 0;
-    if (lane == 0) tail = ld_acquire_gpu(&ctl->tail_copy[(blockIdx.x % kTailCopies) * kTailStride]);
-    tail = __shfl_sync(0xffffffffu, tail, 0);
-    const unsigned long long pub = tail > t0 ? min(tail - t0, 8ull) : 0ull;  // published tickets of the chunk
+    // The tail is acquired again only when the last one seen does not cover
+    // the chunk: requests below a tail already acquired are visible to this
+    // warp (the ring is read with volatile loads, past L1), and every gpu-scope
+    // acquire also costs the SM's L1 the rows the joins had cached there.
+    if (seen < t0 + 8) {
+      unsigned long long tail = 0;
+      if (lane == 0) tail = ld_acquire_gpu(&ctl->tail_copy[(blockIdx.x % kTailCopies) * kTailStride]);
+      seen = __shfl_sync(0xffffffffu, tail, 0);
+    }
+    const unsigned long long pub = seen > t0 ? min(seen - t0, 8ull) : 0ull;  // published tickets of the chunk
     if (pub > (unsigned long long)got) {
       backoff = 64;
       const int cnt = (int)pub - got;
