@@ -335,7 +335,7 @@ typedef struct hsdl_server hsdl_server;
 
 typedef struct hsdl_serve_opts {
   int32_t struct_size;  /* sizeof(hsdl_serve_opts) */
-  int32_t ctas;         /* blocks of the persistent kernel (0 = 4 per SM; at most what fits at once) */
+  int32_t ctas;         /* blocks of the persistent kernel (0 = 6 per SM; at most what fits at once) */
   int32_t ring_log2;    /* request/answer ring capacity = 2^ring_log2 */
   int32_t max_indexes;  /* graph slots */
   int64_t budget_bytes; /* admission budget for resident + pending label bytes */
