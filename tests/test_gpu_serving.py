@@ -162,3 +162,25 @@ def test_mixed_key_formats_in_one_warp(orc, lanes):
     for ix, d in zip(idxs, devs):
         ix.close()
         d.close()
+
+
+@pytest.mark.parametrize("ctas,ring_log2", [(1, 12), (3, 12), (0, 16)])
+def test_pooled_chunks_few_blocks_and_ring_wraps(ctas, ring_log2):
+    """The warps of a block pool their chunks of 8 tickets.  One block (the
+    dispatcher's, 7 workers), three blocks (7 + 8 + 8 workers) and the default
+    grid, with a ring the Poisson run wraps many times: every answer equals the
+    batched path's, in a closed batch and under Poisson arrivals."""
+    K = 5
+    g = H.HostGraph.chung_lu(10000, 8, 2.2, 800, 1, 100, seed=71)
+    dev = H.Graph(g)
+    ix = H.Index.build(dev, K)
+    srv = H.Server(ctas=ctas, ring_log2=ring_log2)
+    gid = srv.add_index(ix)
+    rng = np.random.default_rng(ctas + 7)
+    s, t, k = _queries(rng, g.n, 50000, K)
+    want = ix.query(s, t, k)
+    m = min(len(s), (1 << ring_log2) - 64)  # a closed batch must fit the ring (answers are read after it)
+    assert np.array_equal(srv.query(np.full(m, gid, np.int32), s[:m], t[:m], k[:m]), want[:m])
+    r = srv.loadgen(np.full(len(s), gid, np.int32), s, t, k, offered_qps=2e6, seed=ctas + 1)
+    assert r["completed"] == len(s) and np.array_equal(r["answers"], want)
+    srv.close()
